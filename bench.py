@@ -1,0 +1,446 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 periodic pseudospectral step.
+
+Workload (one "step" = one ETD-RK4 step of the reference scheme, including
+the CFL pass): random isotropic turbulence, von Karman spectrum kp=4, E=0.5,
+xorshift64 seed 42, N=256 (3/2-padded to 384^3), nu=1e-3, adaptive CFL 0.5,
+shell spectrum E(k) every 10 steps.  Inputs are synthetic (seeded).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm prints one JSON line with the FP64 form as the headline (`value`,
+steps/s over all ranks), the FP32-bulk form beside it, the roofline of the
+dominant kernel, the end-to-end rate through the C ABI with host buffers, and
+the CPU restatement timed on this host.  The reference arm (`--impl
+reference`) times the CPU restatement of the reference's path with all host
+threads on the same workload.  Multi-GPU: the path does not shard on one box
+(replicas only), so N ranks run N independent replicas.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "ETD-RK4 steps/s, random isotropic N=256 (FP64 form; FP32-bulk beside it)"
+WORKLOAD = ("random isotropic von Karman E(k)~(k/kp)^4/(1+(k/kp)^2)^(17/6), kp=4, E=0.5, xorshift64 seed 42, "
+            "N=256 (3/2-padded 384^3), nu=1e-3, adaptive CFL 0.5, E(k) every 10 steps")
+HBM_FALLBACK_GBS = 6800.0  # measured copy bandwidth of the GB300s (MEASURED_PEAKS.json hbm_gbs)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--spectrum-every", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only: barrier and max-over-ranks timing)
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 10:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return float("nan")
+
+        load = [r for r in rows if num(r[9]) >= 50.0] or rows
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for i, nm in enumerate(names):
+                if r[5 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(num(r[1]) for r in load), "sm_max_mhz": max(num(r[2]) for r in rows),
+                "power_w_max": max(num(r[3]) for r in rows), "samples": len(rows),
+                "samples_under_load": len(load), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic byte / flop model of the fused schedule (complex elements
+# x element size; per launch)
+# ---------------------------------------------------------------------------
+def pass_model(n: int) -> dict:
+    """Algorithmic complex-element traffic (reads + writes) and flops of one
+    launch of each pass at grid n.  FFT flops: 5 L log2 L per complex line."""
+    h = n // 2 + 1
+    m = 3 * n // 2
+    nh, mnh, mmh = n * n * h, m * n * h, m * m * h
+    lf = 5.0 * m * math.log2(m)   # flops per complex line of length m
+    nf = 5.0 * n * math.log2(n)
+    return {
+        "P1_x_inverse_pad_curl": (3 * nh + 5 * mnh, 5 * n * h * lf),
+        "P2_y_inverse_pad_omega": (5 * mnh + 6 * mmh, 6 * m * h * lf),
+        "P3_z_c2r_cross_r2c": (6 * mmh + 3 * mmh, 4.5 * m * m * lf + 9.0 * m * m * m),
+        "P4_y_forward_trunc": (3 * mmh + 3 * mnh, 3 * m * h * lf),
+        # stage epilogue average over the four ETD stages: (6 + 9 + 12 + 6)/4 = 8.25 N^2H reads+writes
+        "P5_x_forward_trunc_leray_stage": (3 * mnh + 8.25 * nh, 3 * n * h * lf),
+        "NX_ngrid_x_inverse": (6 * nh, 3 * n * h * nf),
+        "NY_ngrid_y_inverse": (6 * nh, 3 * n * h * nf),
+        "NZ_ngrid_z_c2r_max": (3 * nh, 1.5 * n * n * nf),
+    }
+
+
+def step_bytes(n: int, elem: int) -> float:
+    mdl = pass_model(n)
+    per = sum(mdl[k][0] for k in ("P1_x_inverse_pad_curl", "P2_y_inverse_pad_omega", "P3_z_c2r_cross_r2c",
+                                  "P4_y_forward_trunc", "P5_x_forward_trunc_leray_stage")) * 4
+    per += sum(mdl[k][0] for k in ("NX_ngrid_x_inverse", "NY_ngrid_y_inverse", "NZ_ngrid_z_c2r_max"))
+    return per * elem
+
+
+def measured_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        v = float(json.load(open(p))["hbm_gbs"])
+        return v, "measured (MEASURED_PEAKS.json)"
+    except Exception:
+        return HBM_FALLBACK_GBS, "measured (this pool's GB300 copy bandwidth, MEASURED_PEAKS.json hbm_gbs)"
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement timing (reference arm and cpu_baseline)
+# ---------------------------------------------------------------------------
+def time_cpu(u0, n, nu, warmup: int, steps: int, threads: int):
+    from oracle import vk_cpu
+
+    vk_cpu.set_threads(threads)
+    s = vk_cpu.CpuSolver(n, nu, u0)
+    for _ in range(warmup):
+        s.step(1)
+    t0 = time.perf_counter()
+    s.step(steps)
+    el = time.perf_counter() - t0
+    s.close()
+    return el
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, d: Dist):
+    if d.rank != 0:
+        return
+    from vonkarman_gb300 import ics
+
+    n, nu = args.n, 1e-3
+    u0 = ics.von_karman_isotropic(n, kp=4.0, energy=0.5, seed=42)
+    cores = host_cores()
+    # bounded sample: a full CPU step at N=256 takes tens of seconds, so at most
+    # 3 timed steps after at most 1 warm-up step keep the run within minutes
+    ksteps = max(1, min(args.steps, 3))
+    kwarm = min(args.warmup, 1)
+    el = time_cpu(u0, n, nu, kwarm, ksteps, cores)
+    v = ksteps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / ksteps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "precision": "fp64", "replicas": 1},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{ksteps} full ETD-RK4 steps after {kwarm} warm-up step(s), "
+                                   f"C restatement of the reference's CPU path (oracle/vk_cpu.c), OpenMP"},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def pinned_like(lib, shape):
+    nbytes = int(np.prod(shape)) * 16
+    p = ctypes.c_void_p()
+    if lib.vk_pinned_alloc(nbytes, ctypes.byref(p)) != 0:
+        raise RuntimeError("pinned allocation failed")
+    buf = (ctypes.c_char * nbytes).from_address(p.value)
+    arr = np.frombuffer(buf, dtype=np.complex128).reshape(shape)
+    return arr, p
+
+
+def timed_run(s, steps: int, spec_every: int):
+    """steps ETD-RK4 steps with E(k) every spec_every steps, device-timed with
+    CUDA events on the solver's stream."""
+    from vonkarman_gb300 import energy_spectrum
+
+    s.event_mark(0)
+    done = 0
+    specs = 0
+    while done < steps:
+        k = min(spec_every, steps - done) if spec_every > 0 else steps - done
+        s.step(k)
+        done += k
+        if spec_every > 0 and done % spec_every == 0:
+            energy_spectrum(s)
+            specs += 1
+    s.event_mark(1)
+    return s.event_elapsed(0, 1), specs
+
+
+def run_ours(args, d: Dist):
+    import vonkarman_gb300 as vk
+    from vonkarman_gb300 import ics
+    from vonkarman_gb300.solver import probe_fma_peak
+
+    n, nu = args.n, 1e-3
+    dev = d.local
+    u0 = ics.von_karman_isotropic(n, kp=4.0, energy=0.5, seed=42)
+    grid = vk.GridSpec(n)
+    s = vk.Periodic3D(grid, nu, u0, vk.SolverOptions(precision="fp64", device=dev))
+    s.step(args.warmup)
+    s.dt()  # synchronise
+    d.barrier()
+    clk = ClockSampler(dev)
+    clk.start()
+    ms, nspec = timed_run(s, args.steps, args.spectrum_every)
+    clocks = clk.stop()
+    d.barrier()
+    ms = d.max(ms)
+    sps_rank = args.steps / (ms / 1e3)
+    value = d.world * args.steps / (ms / 1e3)
+
+    # per-pass profile (separate run, events around every launch)
+    s.profile(True)
+    prof_steps = 2
+    s.step(prof_steps)
+    prof = s.profile_read()
+    s.profile(False)
+    launches_per_step = sum(c for k, (t, c) in prof.items() if k not in ("spectrum", "tier1_sums")) / prof_steps
+    gpu_launches = int(round(launches_per_step * args.steps)) + 2 * nspec
+
+    mdl = pass_model(n)
+    elem = 16
+    dom = max((k for k in mdl if prof.get(k, (0, 0))[1] > 0), key=lambda k: prof[k][0])
+    dom_ms = prof[dom][0] / prof[dom][1]
+    hbm, hbm_src = measured_hbm()
+    dom_bytes = mdl[dom][0] * elem
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    fp64_peak = probe_fma_peak(dev, True)
+    dom_gflops = mdl[dom][1] / (dom_ms * 1e-3) / 1e9
+    passes = {k: {"ms_per_launch": (t / c if c else None), "launches": c, "share": None}
+              for k, (t, c) in prof.items() if c}
+    tot = sum(t for t, c in prof.values())
+    for k in passes:
+        passes[k]["share"] = prof[k][0] / tot if tot else None
+    sb = step_bytes(n, elem)
+    fp64_res = {}
+    if d.rank == 0:
+        t1 = s.tier1()
+        _, spec64 = vk.energy_spectrum(s)
+        fp64_res = dict(energy=t1.energy, enstrophy=t1.enstrophy, max_vorticity=t1.max_vorticity, spec=spec64,
+                        step=t1.step)
+
+    # end to end through the C ABI with pinned host buffers: every step
+    # uploads the state, steps once and reads the new state back
+    e2e = None
+    if not args.no_e2e:
+        lib = s._lib
+        shp = grid.spectral_shape
+        bufs = [pinned_like(lib, shp) for _ in range(3)]
+        host = [b[0] for b in bufs]
+        for c in range(3):
+            host[c][...] = u0[c]
+        e = vk.Periodic3D(grid, nu, u0, vk.SolverOptions(precision="fp64", device=dev))
+        t_sim, dt_sim = e.time(), e.dt()
+        e.step(1)
+        d.barrier()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            e.restore_state(host, t_sim, i, dt_sim)
+            e.step(1)
+            lib.vk_get_state_host(e._ctx, *[h.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for h in host])
+            if args.spectrum_every > 0 and (i + 1) % args.spectrum_every == 0:
+                vk.energy_spectrum(e)
+        el = d.max(time.perf_counter() - t0)
+        nbytes = 3 * int(np.prod(shp)) * 16
+        e2e = {"value": d.world * args.steps / el, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes,
+               "path": "vk_restore_host + vk_step + vk_get_state_host per step (pinned host buffers)"}
+        e.close()
+        for _, p in bufs:
+            lib.vk_pinned_free(p)
+    s.close()
+
+    # FP32-bulk form on the same workload
+    fp32 = None
+    if not args.no_fp32:
+        s32 = vk.Periodic3D(grid, nu, u0, vk.SolverOptions(precision="fp32bulk", device=dev))
+        s32.step(args.warmup)
+        s32.dt()
+        d.barrier()
+        ms32, _ = timed_run(s32, args.steps, args.spectrum_every)
+        ms32 = d.max(ms32)
+        s32.profile(True)
+        s32.step(prof_steps)
+        prof32 = s32.profile_read()
+        s32.profile(False)
+        dom32 = max((k for k in mdl if prof32.get(k, (0, 0))[1] > 0), key=lambda k: prof32[k][0])
+        d32_ms = prof32[dom32][0] / prof32[dom32][1]
+        fp32 = {"steps_per_s": d.world * args.steps / (ms32 / 1e3), "ms_per_step": ms32 / args.steps,
+                "speedup_vs_fp64": ms / ms32, "hbm_gbs_step": step_bytes(n, 8) / (ms32 / args.steps * 1e-3) / 1e9,
+                "dominant_kernel": dom32,
+                "dominant_roofline": {"bound": "hbm", "achieved": mdl[dom32][0] * 8 / (d32_ms * 1e-3) / 1e9,
+                                      "peak": hbm, "unit": "GB/s",
+                                      "frac": mdl[dom32][0] * 8 / (d32_ms * 1e-3) / 1e9 / hbm}}
+        if d.rank == 0 and fp64_res:
+            t32 = s32.tier1()
+            _, spec32 = vk.energy_spectrum(s32)
+            assert t32.step == fp64_res["step"]
+            rel = lambda a, b: abs(a - b) / max(abs(b), 1e-300)  # noqa: E731
+            sp = fp64_res["spec"]
+            fp32["error_vs_fp64_gpu"] = {
+                "after_steps": int(t32.step),
+                "energy": rel(t32.energy, fp64_res["energy"]),
+                "enstrophy": rel(t32.enstrophy, fp64_res["enstrophy"]),
+                "max_vorticity": rel(t32.max_vorticity, fp64_res["max_vorticity"]),
+                "spectrum_max_rel_shell": float(np.max(np.abs(spec32 - sp)[sp > 1e-12 * sp.max()] /
+                                                       sp[sp > 1e-12 * sp.max()])),
+            }
+        s32.close()
+
+    cpu = None
+    if d.rank == 0 and d.world == 1 and not args.no_cpu_baseline:
+        cores = host_cores()
+        el = time_cpu(u0, n, nu, 0, 1, cores)
+        cpu = {"value": 1.0 / el, "unit": "steps/s", "cores": cores, "kind": "port",
+               "sample": "1 full ETD-RK4 step (incl. CFL and ETD tabulation) at N=256 from the same IC, "
+                         "C restatement of the reference's CPU path (oracle/vk_cpu.c), OpenMP"}
+
+    if d.rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": d.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "precision": "fp64", "replicas": d.world,
+                   "l2": "no flush needed: every pass streams >= 0.9 GB (P2 writes 6x384x384x129x16 B = 1.8 GB) "
+                         "through the 129 MB L2", "timing": "CUDA events on the solver stream"},
+        "hbm_gbs_step": sb / (ms / args.steps * 1e-3) / 1e9,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_source": hbm_src,
+                     "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
+        "fp64_roofline": {"kernel": dom, "achieved": dom_gflops, "peak": fp64_peak, "unit": "GFLOP/s",
+                          "frac": dom_gflops / fp64_peak, "peak_source": "measured live (FP64 FMA probe)",
+                          "note": "the FP64 form is bound by GB300's FP64 pipe, not HBM"},
+        "passes": passes,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": gpu_launches,
+        "clocks": clocks,
+        "fp32bulk": fp32,
+        "sps_per_rank": sps_rank,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    d = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, d)
+        else:
+            run_ours(args, d)
+    finally:
+        d.close()
+
+
+if __name__ == "__main__":
+    main()

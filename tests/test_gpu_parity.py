@@ -1,0 +1,275 @@
+"""GPU parity: the CUDA path (through the C ABI) against the numpy oracle on
+the same inputs.  Norm-relative errors: ||a - b||_2 / ||b||_2 over all
+components (element-wise relative error is ill-posed for the ~0 modes).
+
+Tolerances (FP64): 1e-12 for spectral coefficients after one step or one
+nonlinear evaluation, 1e-10 for Tier-1 diagnostics and E(k); FP32-bulk: 2e-5
+(one step) against the FP64 oracle.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from oracle import vk_oracle as vo
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL_DIAG = 1e-10
+TOL32 = 2e-5
+
+
+def nrel(a, b):
+    num = math.sqrt(sum(float(np.sum(np.abs(x - y) ** 2)) for x, y in zip(a, b)))
+    den = math.sqrt(sum(float(np.sum(np.abs(y) ** 2)) for y in b))
+    return num / den if den > 0 else num
+
+
+def rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def vk():
+    import vonkarman_gb300 as vk
+
+    return vk
+
+
+def random_state(n, seed, clean=True):
+    g = vo.Grid(n)
+    u = vo.random_field(g, seed)
+    if clean:
+        u = vo.hermitian_clean(g, u)
+    return u
+
+
+# --- FftBackend contract (backend.rs:9-25; ndrustfft_backend.rs:75-147) -----
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (16, 16, 16), (32, 32, 32), (64, 64, 64), (12, 12, 12),
+                                   (24, 24, 24), (96, 96, 96), (16, 24, 32), (48, 8, 12), (128, 128, 128)])
+def test_fft_r2c_c2r_vs_numpy(vk, shape):
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(shape)
+    f = vk.GpuFftBackend(*shape)
+    xh = f.r2c_3d(x)
+    ref = np.fft.rfftn(x)
+    assert nrel([xh], [ref]) < TOL64
+    back = f.c2r_3d(xh)
+    assert np.abs(back - x).max() < 1e-12 * max(1.0, np.abs(x).max())
+    # c2r of a non-Hermitian input: imaginary parts of DC/Nyquist planes ignored
+    yh = ref + 0.3j * rng.standard_normal(ref.shape)
+    got = f.c2r_3d(yh)
+    want = np.fft.irfftn(yh, s=shape, axes=(0, 1, 2))
+    assert np.abs(got - want).max() < 1e-12 * np.abs(want).max()
+    f.close()
+
+
+def test_fft_roundtrip_and_parseval_kats(vk):
+    # ndrustfft_backend.rs:75-106 (roundtrip 1e-12) and :108-147 (Parseval 1e-10)
+    n = 8
+    x = np.sin(2 * np.pi * np.arange(n) / n)[:, None, None] * np.ones((n, n, n))
+    f = vk.GpuFftBackend(n, n, n)
+    assert np.abs(f.c2r_3d(f.r2c_3d(x)) - x).max() < 1e-12
+    n = 16
+    i = np.arange(n)
+    x = (np.sin(2 * np.pi * i / n)[:, None, None] + np.cos(2 * np.pi * i / n)[None, :, None]) * np.ones((n, n, n))
+    f = vk.GpuFftBackend(n, n, n)
+    s = f.r2c_3d(x)
+    w = np.full(n // 2 + 1, 2.0)
+    w[0] = w[-1] = 1.0
+    spec = float((w * np.abs(s) ** 2).sum()) / n ** 3
+    assert abs(float((x * x).sum()) - spec) / float((x * x).sum()) < 1e-10
+    assert f.name() and f.precision_digits() == 15
+
+
+def test_fft_fp32_backend(vk):
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((64, 64, 64))
+    f = vk.GpuFftBackend(64, 64, 64, precision="fp32bulk")
+    assert nrel([f.r2c_3d(x)], [np.fft.rfftn(x)]) < 1e-6
+    assert f.precision_digits() == 6
+
+
+# --- compute_nonlinear (nonlinear.rs:15-39, dealiased.rs:16-110) -------------
+
+@pytest.mark.parametrize("n", [8, 16, 32, 64])
+def test_nonlinear_vs_oracle(vk, n):
+    g = vo.Grid(n)
+    u = random_state(n, 10 + n)
+    want = vo.compute_nonlinear(vo.SpectralOps(g), u)
+    s = vk.Periodic3D(vk.GridSpec(n), 0.01, u, vk.SolverOptions(dt_mode="fixed", dt_fixed=1e-3))
+    got = vk.compute_nonlinear(s, u)
+    assert nrel(got, want) < TOL64
+    s.close()
+
+
+def test_nonlinear_non_hermitian_input(vk):
+    # raw random spectral data (not Hermitian in the kz=0 plane): the padded
+    # c2r must drop exactly what the reference's backend drops
+    n = 16
+    g = vo.Grid(n)
+    u = random_state(n, 7, clean=False)
+    want = vo.compute_nonlinear(vo.SpectralOps(g), u)
+    s = vk.Periodic3D(vk.GridSpec(n), 0.01, u, vk.SolverOptions(dt_mode="fixed", dt_fixed=1e-3))
+    assert nrel(vk.compute_nonlinear(s, u), want) < TOL64
+
+
+def test_nonlinear_divergence_free_kat(vk):
+    # nonlinear.rs:50-97: |k . N_hat| < 1e-6 for Taylor-Green at N=16
+    n = 16
+    g = vo.Grid(n)
+    ops = vo.SpectralOps(g)
+    u = vo.taylor_green(g)
+    s = vk.Periodic3D(vk.GridSpec(n), 0.01, u)
+    nl = vk.compute_nonlinear(s, u)
+    div = ops.KX * nl[0] + ops.KY * nl[1] + ops.KZ * nl[2]
+    assert np.abs(div).max() < 1e-6
+
+
+def test_dealiased_zero_and_antisymmetry_kats(vk):
+    # dealiased.rs:173-202 (zero in -> zero out).  The anti-symmetry KAT
+    # (:204-263) is a property of the cross product itself; here the same
+    # P1..P5 chain is checked against the oracle for a single-mode state.
+    n = 8
+    g = vo.Grid(n)
+    z = [np.zeros(g.spectral_shape, complex) for _ in range(3)]
+    s = vk.Periodic3D(vk.GridSpec(n), 0.01, z, vk.SolverOptions(dt_mode="fixed", dt_fixed=1e-3))
+    for c in vk.compute_nonlinear(s, z):
+        assert np.abs(c).max() < 1e-14
+    u = [np.zeros(g.spectral_shape, complex) for _ in range(3)]
+    u[0][1, 2, 1] = 3.0 + 1.0j
+    u[1][n - 2, 1, 3] = -2.0 + 0.5j
+    u[2][3, n - 1, 4] = 1.5 - 0.7j  # z-Nyquist plane (iz = n/2)
+    want = vo.compute_nonlinear(vo.SpectralOps(g), u)
+    assert nrel(vk.compute_nonlinear(s, u), want) < TOL64
+
+
+# --- one step / many steps ---------------------------------------------------
+
+def test_one_step_taylor_green_n64_fixed_dt(vk):
+    # the CPU-runnable Taylor-Green case: N=64, nu=6.25e-4, fixed dt=1e-3
+    n, nu, dt = 64, 6.25e-4, 1e-3
+    g = vo.Grid(n)
+    u0 = vo.taylor_green(g)
+    ref = vo.Periodic3D(g, nu, u0, dt_mode="fixed", dt_fixed=dt)
+    ref.step()
+    s = vk.Periodic3D(vk.GridSpec(n), nu, u0, vk.SolverOptions(dt_mode="fixed", dt_fixed=dt))
+    s.step()
+    assert nrel(s.u_hat(), ref.u_hat) < TOL64
+    assert s.time() == pytest.approx(dt, rel=0, abs=0)
+
+
+@pytest.mark.parametrize("n", [16, 32])
+def test_steps_random_cfl_vs_oracle(vk, n):
+    g = vo.Grid(n)
+    u0 = vo.hermitian_clean(g, vo.random_field(g, 3, amp=float(n) ** 3 / 40.0))
+    nu = 0.02
+    ref = vo.Periodic3D(g, nu, u0)
+    s = vk.Periodic3D(vk.GridSpec(n), nu, u0)
+    assert rel(s.dt(), ref.dt) < 1e-13
+    for _ in range(5):
+        ref.step()
+    s.step(5)
+    assert nrel(s.u_hat(), ref.u_hat) < 1e-11
+    assert rel(s.dt(), ref.dt) < 1e-12
+    assert rel(s.time(), ref.time) < 1e-12
+    assert s.step_count() == 5
+
+
+@pytest.mark.parametrize("variant", ["reference", "cox-matthews"])
+def test_etd_variants_vs_oracle(vk, variant):
+    n = 16
+    g = vo.Grid(n)
+    u0 = vo.taylor_green(g)
+    ref = vo.Periodic3D(g, 0.05, u0, dt_mode="fixed", dt_fixed=0.01, etd_variant=variant)
+    s = vk.Periodic3D(vk.GridSpec(n), 0.05, u0, vk.SolverOptions(dt_mode="fixed", dt_fixed=0.01,
+                                                                   etd_variant=variant))
+    for _ in range(3):
+        ref.step()
+    s.step(3)
+    assert nrel(s.u_hat(), ref.u_hat) < TOL64
+
+
+def test_rk4_vs_oracle(vk):
+    n = 16
+    g = vo.Grid(n)
+    u0 = vo.hermitian_clean(g, vo.random_field(g, 5, amp=50.0))
+    ref = vo.Periodic3D(g, 0.01, u0, dt_mode="fixed", dt_fixed=1e-3, integrator="rk4")
+    s = vk.Periodic3D(vk.GridSpec(n), 0.01, u0, vk.SolverOptions(dt_mode="fixed", dt_fixed=1e-3,
+                                                                   integrator="rk4"))
+    for _ in range(3):
+        ref.step()
+    s.step(3)
+    assert nrel(s.u_hat(), ref.u_hat) < TOL64
+
+
+def test_tier1_and_spectrum_vs_oracle(vk):
+    n = 32
+    g = vo.Grid(n)
+    u0 = vo.hermitian_clean(g, vo.random_field(g, 9, amp=200.0))
+    ref = vo.Periodic3D(g, 0.01, u0)
+    s = vk.Periodic3D(vk.GridSpec(n), 0.01, u0)
+    for _ in range(3):
+        ref.step()
+    s.step(3)
+    want = ref.tier1()
+    got = s.tier1()
+    for k, v in want.items():
+        if k == "step":
+            assert got.step == v
+            continue
+        tol = TOL_DIAG if k != "helicity" else 1e-9
+        assert abs(getattr(got, k) - v) <= tol * max(abs(v), 1e-300) + 1e-13, k
+    shells, spec = vk.energy_spectrum(s)
+    sh_ref, spec_ref = vo.energy_spectrum(ref.u_hat, ref.ops)
+    assert np.array_equal(shells, sh_ref)
+    assert np.abs(spec - spec_ref).max() <= TOL_DIAG * np.abs(spec_ref).max()
+    assert s.cfl_dt() == pytest.approx(ref.compute_cfl_dt(), rel=1e-13)
+
+
+def test_restart_bitwise(vk):
+    # solver.rs:673-706 / tests/checkpoint_restart.rs:10-63
+    n = 16
+    g = vo.Grid(n)
+    u0 = vo.taylor_green(g)
+    cont = vk.Periodic3D(vk.GridSpec(n), 0.01, u0)
+    cont.step(20)
+    half = vk.Periodic3D(vk.GridSpec(n), 0.01, u0)
+    half.step(10)
+    rest = vk.Periodic3D.from_checkpoint(half.checkpoint_data())
+    rest.step(10)
+    for a, b in zip(cont.u_hat(), rest.u_hat()):
+        assert np.array_equal(a, b)
+    assert cont.time() == rest.time() and cont.step_count() == rest.step_count()
+
+
+def test_run_records_match_tier1(vk):
+    n = 16
+    g = vo.Grid(n)
+    u0 = vo.taylor_green(g)
+    a = vk.Periodic3D(vk.GridSpec(n), 0.01, u0)
+    recs = a.run(6, every=2)
+    b = vk.Periodic3D(vk.GridSpec(n), 0.01, u0)
+    for r in recs:
+        b.step(2)
+        t = b.tier1()
+        assert r.step == t.step
+        for k in ("time", "dt", "energy", "enstrophy", "helicity", "superhelicity", "max_vorticity"):
+            assert getattr(r, k) == getattr(t, k), k
+
+
+def test_fp32bulk_one_step(vk):
+    n = 32
+    g = vo.Grid(n)
+    u0 = vo.hermitian_clean(g, vo.random_field(g, 4, amp=100.0))
+    ref = vo.Periodic3D(g, 0.01, u0, dt_mode="fixed", dt_fixed=2e-3)
+    ref.step()
+    s = vk.Periodic3D(vk.GridSpec(n), 0.01, u0, vk.SolverOptions(precision="fp32bulk", dt_mode="fixed",
+                                                                   dt_fixed=2e-3))
+    s.step()
+    assert nrel(s.u_hat(), ref.u_hat) < TOL32
+    e = s.energy()
+    assert rel(e, ref.energy()) < 1e-6

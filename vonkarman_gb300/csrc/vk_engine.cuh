@@ -1,0 +1,287 @@
+// Host-side launchers: map runtime grid sizes onto the compile-time kernel
+// instances.  Instantiated once per precision (vk_engine_f64.cu,
+// vk_engine_f32.cu) so the two compile in parallel.
+#pragma once
+
+#include "vk_reduce.cuh"
+
+namespace vk {
+
+// Per-device cache of the dynamic shared memory opt-in (one bit per device
+// below 64, one cache per kernel instance).  Kernels with static shared
+// memory as well need the opt-in below 48 KB of dynamic memory too, so any
+// sizeable request opts in.
+template <auto KERN>
+inline cudaError_t prepare_kernel(size_t smem) {
+  static unsigned long long done_mask = 0ull;
+  if (smem <= 16 * 1024) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = dev < 64 ? (1ull << dev) : 0ull;
+  if (bit && (done_mask & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(KERN, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) done_mask |= bit;
+  return e;
+}
+
+// ---------------------------------------------------------------------------
+template <typename R, int L, bool INV, int TZ, class Op>
+inline cudaError_t launch_strided(const Op& op, int nblocks, const C2<R>* tw, cudaStream_t s) {
+  constexpr int NT = cmax(64, cmin(1024, round32(TZ * L / 8)));
+  const size_t smem = (size_t)L * TZ * sizeof(C2<R>);
+  constexpr auto kern = k_strided<R, L, INV, TZ, NT, Op>;
+  cudaError_t e = prepare_kernel<kern>(smem);
+  if (e != cudaSuccess) return e;
+  kern<<<nblocks, NT, smem, s>>>(op, tw);
+  return cudaGetLastError();
+}
+
+template <typename R, int N>
+inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
+  constexpr int M = 3 * N / 2;
+  constexpr int H = N / 2 + 1;
+  constexpr int TZ = TZof<R>::value;
+  const int nzt = (H + TZ - 1) / TZ;
+  const size_t fsA1 = (size_t)M * N * H;   // P1 out field stride
+  const size_t fsB2 = (size_t)M * M * H;   // P2 out field stride
+  const size_t fsA3 = (size_t)M * M * H;   // P3 out field stride
+  const size_t fsB4 = (size_t)M * N * H;   // P4 out field stride
+  const R ks = (R)p.ks;
+  cudaError_t e;
+  // P1
+  {
+    TimerScope ts(p.timer, PASS_P1, s);
+    OpXInv<R> o{5, nzt, H, M, N, M, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fsA1};
+    e = launch_strided<R, M, true, TZ>(o, 5 * nzt * N, p.twM, s);
+    if (e != cudaSuccess) return e;
+  }
+  // P2
+  {
+    TimerScope ts(p.timer, PASS_P2, s);
+    OpYInv<R> o{6, nzt, H, M, N, M, 0, ks, p.bufA, fsA1, p.bufB, fsB2};
+    e = launch_strided<R, M, true, TZ>(o, 6 * nzt * M, p.twM, s);
+    if (e != cudaSuccess) return e;
+  }
+  // P3
+  {
+    TimerScope ts(p.timer, PASS_P3, s);
+    constexpr int CP = zpairs<M, 768>();
+    constexpr int NT = zthreads<6 * CP, M>();
+    const size_t smem = (size_t)6 * CP * M * sizeof(C2<R>);
+    constexpr auto kern = k_p3<R, M, CP, NT>;
+    e = prepare_kernel<kern>(smem);
+    if (e != cudaSuccess) return e;
+    P3Args<R> a{M * M, p.bufB, fsB2, p.bufA, fsA3};
+    const int nb = (M * M + 2 * CP - 1) / (2 * CP);
+    kern<<<nb, NT, smem, s>>>(a, p.twM);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  // P4
+  {
+    TimerScope ts(p.timer, PASS_P4, s);
+    OpYFwdTrunc<R> o{3, nzt, H, N, N, M, p.bufA, fsA3, p.bufB, fsB4};
+    e = launch_strided<R, M, false, TZ>(o, 3 * nzt * M, p.twM, s);
+    if (e != cudaSuccess) return e;
+  }
+  // P5
+  {
+    TimerScope ts(p.timer, PASS_P5, s);
+    constexpr int TZ5 = TZ / 2;
+    constexpr int NT = cmax(64, cmin(1024, round32(TZ5 * M / 8)));
+    const int nzt5 = (H + TZ5 - 1) / TZ5;
+    const size_t smem = (size_t)(M + 2 * N) * TZ5 * sizeof(C2<R>);
+    constexpr auto kern = k_p5<R, M, TZ5, NT>;
+    e = prepare_kernel<kern>(smem);
+    if (e != cudaSuccess) return e;
+    const double scale = (double)M * M * M / ((double)N * N * N);
+    P5Args<R> a{N, M, H, nzt5, (R)(1.0 / scale), ks, p.bufB, fsB4, p.st};
+    kern<<<nzt5 * N, NT, smem, s>>>(a, p.twM);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+template <typename R, int N>
+inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
+  constexpr int H = N / 2 + 1;
+  constexpr int TZ = TZof<R>::value;
+  const int nzt = (H + TZ - 1) / TZ;
+  const size_t fs = (size_t)N * N * H;
+  const R ks = (R)p.ks;
+  const bool both = p.which == 3;
+  const bool need_w = p.which != 1;
+  cudaError_t e;
+  {
+    TimerScope ts(p.timer, PASS_NX, s);
+    const int nf = need_w ? 5 : 3;
+    OpXInv<R> o{nf, nzt, H, N, N, N, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fs};
+    e = launch_strided<R, N, true, TZ>(o, nf * nzt * N, p.twN, s);
+    if (e != cudaSuccess) return e;
+  }
+  {
+    TimerScope ts(p.timer, PASS_NY, s);
+    const int nf = both ? 6 : 3;
+    const int gbase = p.which == 2 ? 3 : 0;
+    OpYInv<R> o{nf, nzt, H, N, N, N, gbase, ks, p.bufA, fs, p.bufB, fs};
+    e = launch_strided<R, N, true, TZ>(o, nf * nzt * N, p.twN, s);
+    if (e != cudaSuccess) return e;
+  }
+  TimerScope ts(p.timer, PASS_NZ, s);
+  constexpr int CP = zpairs<N, 512>();
+  NZArgs<R> a{N * N, p.bufB, fs, p.out, p.which};
+  const int nb = (N * N + 2 * CP - 1) / (2 * CP);
+  if (both) {
+    constexpr int NT = zthreads<6 * CP, N>();
+    const size_t smem = (size_t)6 * CP * N * sizeof(C2<R>);
+    constexpr auto kern = k_nz_max<R, N, CP, true, NT>;
+    e = prepare_kernel<kern>(smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nb, NT, smem, s>>>(a, p.twN);
+  } else {
+    constexpr int NT = zthreads<3 * CP, N>();
+    const size_t smem = (size_t)3 * CP * N * sizeof(C2<R>);
+    constexpr auto kern = k_nz_max<R, N, CP, false, NT>;
+    e = prepare_kernel<kern>(smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nb, NT, smem, s>>>(a, p.twN);
+  }
+  return cudaGetLastError();
+}
+
+// Standalone backend: one pass per axis with its own length.
+template <typename R, int L>
+inline cudaError_t fz_pass(const FftParams<R>& p, bool inverse, R scale, cudaStream_t s) {
+  constexpr int CP = zpairs<L, 4096>();
+  constexpr int NT = zthreads<CP, L>();
+  const size_t smem = (size_t)CP * L * sizeof(C2<R>);
+  const int ncols = p.nx * p.ny;
+  const int nb = (ncols + 2 * CP - 1) / (2 * CP);
+  FZArgs<R> a{ncols, p.real, p.cplx, scale};
+  cudaError_t e;
+  if (inverse) {
+    constexpr auto kern = k_fz_c2r<R, L, CP, NT>;
+    e = prepare_kernel<kern>(smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nb, NT, smem, s>>>(a, p.twz);
+  } else {
+    constexpr auto kern = k_fz_r2c<R, L, CP, NT>;
+    e = prepare_kernel<kern>(smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nb, NT, smem, s>>>(a, p.twz);
+  }
+  return cudaGetLastError();
+}
+
+template <typename R, int L, int AXIS>
+inline cudaError_t fxy_pass(const FftParams<R>& p, bool inverse, cudaStream_t s) {
+  constexpr int TZ = TZof<R>::value;
+  const int hz = p.nz / 2 + 1;
+  const int nzt = (hz + TZ - 1) / TZ;
+  OpPlainC2C<R, AXIS> o{1, nzt, hz, L, p.nx, p.ny, p.cplx};
+  const int nouter = AXIS == 0 ? p.ny : p.nx;
+  const C2<R>* tw = AXIS == 0 ? p.twx : p.twy;
+  if (inverse) return launch_strided<R, L, true, TZ>(o, nzt * nouter, tw, s);
+  return launch_strided<R, L, false, TZ>(o, nzt * nouter, tw, s);
+}
+
+#define VK_FOR_LENGTHS(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(12) X(24) X(48) X(96) X(192) X(384) X(768)
+
+template <typename R>
+inline cudaError_t fz_dispatch(const FftParams<R>& p, bool inverse, R scale, cudaStream_t s) {
+  switch (p.nz) {
+#define VK_CASE(L) case L: return fz_pass<R, L>(p, inverse, scale, s);
+    VK_FOR_LENGTHS(VK_CASE)
+#undef VK_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename R, int AXIS>
+inline cudaError_t fxy_dispatch(const FftParams<R>& p, bool inverse, cudaStream_t s) {
+  const int L = AXIS == 0 ? p.nx : p.ny;
+  switch (L) {
+#define VK_CASE(LL) case LL: return fxy_pass<R, LL, AXIS>(p, inverse, s);
+    VK_FOR_LENGTHS(VK_CASE)
+#undef VK_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+#define VK_FOR_GRIDS(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512)
+
+template <typename R>
+cudaError_t Engine<R>::nle(const NleParams<R>& p, cudaStream_t s) {
+  switch (p.N) {
+#define VK_CASE(NN) case NN: return nle_n<R, NN>(p, s);
+    VK_FOR_GRIDS(VK_CASE)
+#undef VK_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename R>
+cudaError_t Engine<R>::ngrid_max(const NgridParams<R>& p, cudaStream_t s) {
+  switch (p.N) {
+#define VK_CASE(NN) case NN: return ngrid_n<R, NN>(p, s);
+    VK_FOR_GRIDS(VK_CASE)
+#undef VK_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename R>
+cudaError_t Engine<R>::fft_r2c(const FftParams<R>& p, cudaStream_t s) {
+  cudaError_t e;
+  {
+    TimerScope ts(p.timer, PASS_FFT_Z, s);
+    e = fz_dispatch<R>(p, false, R(1), s);
+  }
+  if (e != cudaSuccess) return e;
+  {
+    TimerScope ts(p.timer, PASS_FFT_Y, s);
+    e = fxy_dispatch<R, 1>(p, false, s);
+  }
+  if (e != cudaSuccess) return e;
+  TimerScope ts(p.timer, PASS_FFT_X, s);
+  return fxy_dispatch<R, 0>(p, false, s);
+}
+
+template <typename R>
+cudaError_t Engine<R>::fft_c2r(const FftParams<R>& p, cudaStream_t s) {
+  cudaError_t e;
+  {
+    TimerScope ts(p.timer, PASS_FFT_X, s);
+    e = fxy_dispatch<R, 0>(p, true, s);
+  }
+  if (e != cudaSuccess) return e;
+  {
+    TimerScope ts(p.timer, PASS_FFT_Y, s);
+    e = fxy_dispatch<R, 1>(p, true, s);
+  }
+  if (e != cudaSuccess) return e;
+  const R scale = (R)(1.0 / ((double)p.nx * p.ny * p.nz));
+  TimerScope ts(p.timer, PASS_FFT_Z, s);
+  return fz_dispatch<R>(p, true, scale, s);
+}
+
+template <typename R>
+cudaError_t Engine<R>::tier1_partial(const C2<R>* u, size_t cs, int N, double ks, double* part, int nblk,
+                                     cudaStream_t s) {
+  k_tier1_partial<R><<<nblk, RED_THREADS, 0, s>>>(u, cs, N, N / 2 + 1, ks, part);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t Engine<R>::spectrum_partial(const C2<R>* u, size_t cs, int N, double ks, int nsh, double* part,
+                                        int nblk, cudaStream_t s) {
+  const size_t smem = (size_t)nsh * sizeof(double);
+  constexpr auto kern = k_spectrum_partial<R>;
+  cudaError_t e = prepare_kernel<kern>(smem);
+  if (e != cudaSuccess) return e;
+  kern<<<nblk, RED_THREADS, smem, s>>>(u, cs, N, N / 2 + 1, ks, nsh, part);
+  return cudaGetLastError();
+}
+
+}  // namespace vk

@@ -1,0 +1,649 @@
+// Pass kernels of the periodic pseudospectral step.
+//
+// Layouts (all complex arrays interleaved {re, im}, z index fastest):
+//   spectral state     (N, N, H)     [ix][iy][iz]     H = N/2 + 1
+//   after P1           (M, N, H) x 5 [x][iy][iz]      M = 3N/2
+//   after P2           (M, M, H) x 6 [x][y][iz]
+//   after P3           (M, M, H) x 3 [x][y][iz]
+//   after P4           (M, N, H) x 3 [x][iy][iz]
+// The spectral state keeps the reference's ndarray C order
+// (vonkarman-core/src/field.rs:48-50), so host upload/download is a copy.
+//
+// One nonlinear evaluation N(u) = P[F(u x curl u)] with 3/2 padding
+// (vonkarman-periodic/src/nonlinear.rs:15-39, vonkarman-fft/src/dealiased.rs:16-110)
+// is the pass chain P1..P5:
+//   P1  x-inverse of u and of i*kx*u_{y,z}, zero-pad N->M along x  (5 fields)
+//   P2  y-inverse with zero-pad, forming u and omega = i k x u     (6 fields)
+//   P3  z: C2R of u, omega (packed pairwise), u x omega, R2C, keep H modes
+//   P4  y-forward, keep N of M modes
+//   P5  x-forward, keep N of M modes, scale, Leray projection, stage epilogue
+// The padded spectral arrays of the reference are never materialised.
+#pragma once
+
+#include "vk_fft.cuh"
+
+namespace vk {
+
+// ---------------------------------------------------------------------------
+// Index helpers
+// ---------------------------------------------------------------------------
+// padded position -> N-grid index, or -1 for a zero-padded slot
+// (inverse of dealiased.rs:129-131)
+__device__ __forceinline__ int unpad_pos(int p, int N, int M) {
+  if (p < N / 2) return p;
+  if (p >= M - N / 2) return p - (M - N);
+  return -1;
+}
+// N-grid index -> padded position (dealiased.rs:129-131, :151-157)
+__device__ __forceinline__ int pad_pos(int i, int N, int M) { return i < N / 2 ? i : M - (N - i); }
+// rfftfreq_full index -> integer wavenumber, n/2 -> -n/2 (spectral_ops.rs:51-63)
+__device__ __forceinline__ int signed_k(int i, int N) { return i < N / 2 ? i : i - N; }
+
+__host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int round32(int a) { return (a + 31) / 32 * 32; }
+
+// Lines per CTA for the strided (x / y) passes: TZ consecutive iz values, so
+// each row segment is 128 bytes.
+template <typename R> struct TZof { static constexpr int value = sizeof(R) == 8 ? 8 : 16; };
+template <typename R, int L>
+__host__ __device__ constexpr int strided_threads() {
+  return cmax(64, cmin(1024, round32(TZof<R>::value * L / 8)));
+}
+// z passes: column pairs per CTA so that CP * L == 768 (z-cross) / 512 (N grid)
+template <int L, int TARGET> __host__ __device__ constexpr int zpairs() { return cmax(1, TARGET / L); }
+template <int NLINES, int L>
+__host__ __device__ constexpr int zthreads() { return cmax(64, cmin(1024, round32(NLINES * L / 8))); }
+
+// ---------------------------------------------------------------------------
+// Generic strided pass: one field of TZ interleaved lines per CTA.
+// blockIdx.x = f + nfields * (ztile + nztiles * outer)
+// ---------------------------------------------------------------------------
+template <typename R, int L, bool INV, int TZ, int NT, class Op>
+__global__ void __launch_bounds__(NT) k_strided(Op op, const C2<R>* __restrict__ tw) {
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  C2<R>* buf = reinterpret_cast<C2<R>*>(vk_smem);
+  const int f = blockIdx.x % op.nfields;
+  const int rest = blockIdx.x / op.nfields;
+  const int zt = rest % op.nztiles;
+  const int outer = rest / op.nztiles;
+  const int z0 = zt * TZ;
+  for (int e = threadIdx.x; e < L * TZ; e += NT) {
+    const int p = e / TZ, b = e % TZ;
+    const int z = z0 + b;
+    buf[e] = (z < op.hz) ? op.load(f, outer, z, p) : czero<R>();
+  }
+  __syncthreads();
+  fft_smem<R, L, INV, NT, TZ, true>(buf, 1, TZ, tw);
+  for (int e = threadIdx.x; e < op.nout * TZ; e += NT) {
+    const int i = e / TZ, b = e % TZ;
+    const int z = z0 + b;
+    if (z < op.hz) op.store(f, outer, z, i, buf[op.src_pos(i) * TZ + b]);
+  }
+}
+
+// P1 / N-grid X: x-inverse of the spectral state, zero-pad N -> M (M == N on
+// the N grid).  Fields: 0..2 = u_c, 3 = i kx u_y, 4 = i kx u_z.  s_in folds the
+// 1/M^3 of the padded c2r and the (M/N)^3 pre-scale (dealiased.rs:43,:45-62)
+// into one factor 1/N^3.
+template <typename R> struct OpXInv {
+  int nfields, nztiles, hz, nout;
+  int N, M;
+  R s_in, ks;
+  const C2<R>* in; size_t cs;
+  C2<R>* out; size_t fs;
+  __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
+    const int ix = unpad_pos(p, N, M);
+    if (ix < 0) return czero<R>();
+    const int c = f < 3 ? f : f - 2;
+    C2<R> v = in[(size_t)c * cs + ((size_t)ix * N + iy) * hz + z];
+    v = cscale<R>(v, s_in);
+    if (f >= 3) {
+      const R kx = ks * (R)signed_k(ix, N);
+      v = cmk<R>(-kx * v.y, kx * v.x);
+    }
+    return v;
+  }
+  __device__ __forceinline__ int src_pos(int i) const { return i; }
+  __device__ __forceinline__ void store(int f, int iy, int z, int i, C2<R> v) const {
+    out[(size_t)f * fs + ((size_t)i * N + iy) * hz + z] = v;
+  }
+};
+
+// P2 / N-grid Y: y-inverse with zero-pad, forming u (g = 0..2) and
+// omega = i k x u (g = 3..5) from the x-transformed fields
+// (curl: vonkarman-core/src/spectral_ops.rs:81-108).  kx was applied in P1, ky
+// and kz are applied here (both are constant along an x line).
+template <typename R> struct OpYInv {
+  int nfields, nztiles, hz, nout;
+  int N, M, gbase;
+  R ks;
+  const C2<R>* in; size_t fsin;   // (M, N, H): Ux, Uy, Uz, Vy, Vz
+  C2<R>* out; size_t fsout;       // (M, M, H)
+  __device__ __forceinline__ C2<R> load(int f, int x, int z, int p) const {
+    const int iy = unpad_pos(p, N, M);
+    if (iy < 0) return czero<R>();
+    const int g = f + gbase;
+    const size_t base = ((size_t)x * N + iy) * hz + z;
+    if (g < 3) return in[(size_t)g * fsin + base];
+    const R ky = ks * (R)signed_k(iy, N);
+    const R kz = ks * (R)z;
+    if (g == 3) {  // i (ky Uz - kz Uy)
+      const C2<R> uy = in[fsin + base], uz = in[2 * fsin + base];
+      const C2<R> t = cmk<R>(ky * uz.x - kz * uy.x, ky * uz.y - kz * uy.y);
+      return cmul_i<R>(t);
+    }
+    if (g == 4) {  // i kz Ux - Vz
+      const C2<R> ux = in[base], vz = in[4 * fsin + base];
+      return cmk<R>(-kz * ux.y - vz.x, kz * ux.x - vz.y);
+    }
+    // g == 5: Vy - i ky Ux
+    const C2<R> ux = in[base], vy = in[3 * fsin + base];
+    return cmk<R>(vy.x + ky * ux.y, vy.y - ky * ux.x);
+  }
+  __device__ __forceinline__ int src_pos(int i) const { return i; }
+  __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
+    out[(size_t)f * fsout + ((size_t)x * M + i) * hz + z] = v;
+  }
+};
+
+// P4: y-forward of the three cross-product fields, keep N of M modes
+// (truncate_spectral, dealiased.rs:141-163).
+template <typename R> struct OpYFwdTrunc {
+  int nfields, nztiles, hz, nout;
+  int N, M;
+  const C2<R>* in; size_t fsin;   // (M, M, H)
+  C2<R>* out; size_t fsout;       // (M, N, H)
+  __device__ __forceinline__ C2<R> load(int f, int x, int z, int p) const {
+    return in[(size_t)f * fsin + ((size_t)x * M + p) * hz + z];
+  }
+  __device__ __forceinline__ int src_pos(int i) const { return pad_pos(i, N, M); }
+  __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
+    out[(size_t)f * fsout + ((size_t)x * N + i) * hz + z] = v;
+  }
+};
+
+// Standalone FFT backend: C2C along x (AXIS 0) or y (AXIS 1) of an
+// (nx, ny, hz) complex array, in place.
+template <typename R, int AXIS> struct OpPlainC2C {
+  int nfields, nztiles, hz, nout;
+  int nx, ny;
+  C2<R>* data;
+  __device__ __forceinline__ size_t at(int outer, int z, int p) const {
+    return AXIS == 0 ? ((size_t)p * ny + outer) * hz + z : ((size_t)outer * ny + p) * hz + z;
+  }
+  __device__ __forceinline__ C2<R> load(int, int outer, int z, int p) const { return data[at(outer, z, p)]; }
+  __device__ __forceinline__ int src_pos(int i) const { return i; }
+  __device__ __forceinline__ void store(int, int outer, int z, int i, C2<R> v) const { data[at(outer, z, i)] = v; }
+};
+
+// ---------------------------------------------------------------------------
+// Stage epilogues (fused into P5).  Reference forms:
+//   ETD-RK4 reference variant  vonkarman-periodic/src/solver.rs:221-379
+//   classical RK4              vonkarman-periodic/src/rk4.rs:16-146
+// ETD coefficients live in a table keyed by the integer |k|^2 index
+// m = kx'^2 + ky'^2 + kz'^2 (8 doubles per entry).
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ C2<R> axpby(R a, C2<R> x, R b, C2<R> y) {
+  return cmk<R>(a * x.x + b * y.x, a * x.y + b * y.y);
+}
+
+template <typename R>
+__device__ __forceinline__ void stage_apply(const StageArgs<R>& s, size_t idx, int m, R k2, const C2<R>* nl) {
+  const size_t cs = s.cs;
+  if (s.op == ST_NL_OUT) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s.out[c * cs + idx] = nl[c];
+    return;
+  }
+  const double dt = *s.dt;
+  if (s.op >= ST_RK4_1) {
+    // rhs = N + (-nu k^2) state  (rk4.rs:30-45)
+    const R visc = (R)(-s.nu) * k2;
+    const bool first = s.op == ST_RK4_1;
+    const R half = (R)(0.5 * dt);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t i = c * cs + idx;
+      const C2<R> u = s.u[i];
+      const C2<R> st = first ? u : s.temp[i];
+      const C2<R> rhs = cmk<R>(nl[c].x + visc * st.x, nl[c].y + visc * st.y);
+      if (s.op == ST_RK4_1) {
+        s.acc[i] = rhs;
+        s.temp[i] = cmk<R>(u.x + half * rhs.x, u.y + half * rhs.y);
+      } else if (s.op == ST_RK4_2 || s.op == ST_RK4_3) {
+        const C2<R> a = s.acc[i];
+        s.acc[i] = cmk<R>(a.x + R(2) * rhs.x, a.y + R(2) * rhs.y);
+        const R h = s.op == ST_RK4_2 ? half : (R)dt;
+        s.temp[i] = cmk<R>(u.x + h * rhs.x, u.y + h * rhs.y);
+      } else {
+        const C2<R> a = s.acc[i];
+        const R sixth = (R)(dt / 6.0);
+        s.u[i] = cmk<R>(u.x + sixth * (a.x + rhs.x), u.y + sixth * (a.y + rhs.y));
+      }
+    }
+    return;
+  }
+  const double* e = s.etd + (size_t)m * ETD_STRIDE;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const size_t i = c * cs + idx;
+    const C2<R> u = s.u[i];
+    const C2<R> n = nl[c];
+    switch (s.op) {
+      case ST_ETD_REF_1: {  // solver.rs:264-281
+        s.n1[i] = n;
+        s.temp[i] = axpby<R>((R)e[E_HALF], u, (R)(dt * e[E_A21]), n);
+        break;
+      }
+      case ST_ETD_REF_2: {  // solver.rs:291-308; acc starts the final sum
+        const C2<R> n1 = s.n1[i];
+        s.acc[i] = axpby<R>((R)e[E_B1], n1, (R)e[E_B23], n);
+        s.temp[i] = axpby<R>((R)e[E_HALF], u, (R)(dt * e[E_A21]), n);
+        break;
+      }
+      case ST_ETD_REF_3: {  // solver.rs:318-344
+        const C2<R> n1 = s.n1[i];
+        const C2<R> a = s.acc[i];
+        const R b23 = (R)e[E_B23];
+        s.acc[i] = cmk<R>(a.x + b23 * n.x, a.y + b23 * n.y);
+        const C2<R> dn = cmk<R>(R(2) * n.x - n1.x, R(2) * n.y - n1.y);
+        s.temp[i] = axpby<R>((R)e[E_FULL], u, (R)(dt * e[E_A41]), dn);
+        break;
+      }
+      case ST_ETD_4: {  // solver.rs:354-378
+        const C2<R> a = s.acc[i];
+        const R b4 = (R)e[E_B4];
+        const C2<R> rhs = cmk<R>(a.x + b4 * n.x, a.y + b4 * n.y);
+        s.u[i] = axpby<R>((R)e[E_FULL], u, (R)dt, rhs);
+        break;
+      }
+      case ST_ETD_CM_1: {  // textbook: a = E2 u + (h/2) phi1(z/2) N1
+        s.n1[i] = n;
+        s.temp[i] = axpby<R>((R)e[E_HALF], u, (R)(0.5 * dt * e[E_A21]), n);
+        break;
+      }
+      case ST_ETD_CM_2: {  // b = E2 u + (h/2) phi1(z/2) N2
+        const C2<R> n1 = s.n1[i];
+        s.acc[i] = axpby<R>((R)e[E_B1], n1, (R)e[E_B23], n);
+        s.temp[i] = axpby<R>((R)e[E_HALF], u, (R)(0.5 * dt * e[E_A21]), n);
+        break;
+      }
+      case ST_ETD_CM_3: {  // c = E2 a + (h/2) phi1(z/2) (2 N3 - N1), a rebuilt from u, N1
+        const C2<R> n1 = s.n1[i];
+        const C2<R> ac = s.acc[i];
+        const R b23 = (R)e[E_B23];
+        s.acc[i] = cmk<R>(ac.x + b23 * n.x, ac.y + b23 * n.y);
+        const R eh = (R)e[E_HALF];
+        const R q = (R)(0.5 * dt * e[E_A21]);
+        const C2<R> a = axpby<R>(eh, u, q, n1);
+        const C2<R> dn = cmk<R>(R(2) * n.x - n1.x, R(2) * n.y - n1.y);
+        s.temp[i] = axpby<R>(eh, a, q, dn);
+        break;
+      }
+      default: break;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// P5: x-forward of the three fields, keep N of M modes, scale by N^3/M^3
+// (dealiased.rs:102-109), Leray projection (spectral_ops.rs:114-151), stage
+// epilogue.  One CTA = one iy and TZ consecutive iz, all three components;
+// shared memory holds the FFT tile (L x TZ) plus two finished components
+// (2 x N x TZ).
+// ---------------------------------------------------------------------------
+template <typename R> struct P5Args {
+  int N, M, H, nztiles;
+  R s_out, ks;
+  const C2<R>* in; size_t fsin;   // (M, N, H)
+  StageArgs<R> st;
+};
+
+template <typename R, int L, int TZ, int NT>
+__global__ void __launch_bounds__(NT) k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
+  constexpr int N = 2 * L / 3;
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  C2<R>* buf = reinterpret_cast<C2<R>*>(vk_smem);
+  C2<R>* keep = buf + L * TZ;
+  const int zt = blockIdx.x % a.nztiles;
+  const int iy = blockIdx.x / a.nztiles;
+  const int z0 = zt * TZ;
+  const int H = a.H;
+  for (int c = 0; c < 3; ++c) {
+    for (int e = threadIdx.x; e < L * TZ; e += NT) {
+      const int p = e / TZ, b = e % TZ;
+      const int z = z0 + b;
+      buf[e] = z < H ? a.in[(size_t)c * a.fsin + ((size_t)p * N + iy) * H + z] : czero<R>();
+    }
+    __syncthreads();
+    fft_smem<R, L, false, NT, TZ, true>(buf, 1, TZ, tw);
+    if (c == 2) break;  // the third field stays in buf
+    for (int e = threadIdx.x; e < N * TZ; e += NT) {
+      const int ix = e / TZ, b = e % TZ;
+      keep[c * N * TZ + e] = buf[pad_pos(ix, N, L) * TZ + b];
+    }
+    __syncthreads();
+  }
+  const int kyi = signed_k(iy, N);
+  const R ky = a.ks * (R)kyi;
+  for (int e = threadIdx.x; e < N * TZ; e += NT) {
+    const int ix = e / TZ, b = e % TZ;
+    const int z = z0 + b;
+    if (z >= H) continue;
+    const int kxi = signed_k(ix, N);
+    const R kx = a.ks * (R)kxi;
+    const R kz = a.ks * (R)z;
+    C2<R> nl[3] = {cscale<R>(keep[e], a.s_out), cscale<R>(keep[N * TZ + e], a.s_out),
+                   cscale<R>(buf[pad_pos(ix, N, L) * TZ + b], a.s_out)};
+    const R k2 = (kx * kx + ky * ky) + kz * kz;
+    if (!(k2 < R(1e-30))) {
+      const R inv = R(1) / k2;
+      const C2<R> kd = cmk<R>((kx * nl[0].x + ky * nl[1].x) + kz * nl[2].x,
+                              (kx * nl[0].y + ky * nl[1].y) + kz * nl[2].y);
+      nl[0] = cmk<R>(nl[0].x - kx * kd.x * inv, nl[0].y - kx * kd.y * inv);
+      nl[1] = cmk<R>(nl[1].x - ky * kd.x * inv, nl[1].y - ky * kd.y * inv);
+      nl[2] = cmk<R>(nl[2].x - kz * kd.x * inv, nl[2].y - kz * kd.y * inv);
+    }
+    const int m = kxi * kxi + kyi * kyi + z * z;
+    stage_apply<R>(a.st, ((size_t)ix * N + iy) * H + z, m, k2, nl);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// z-line helpers.  Two real z lines x, y of length L share one complex line
+// Z = x + i y.  Packing from their half spectra X, Y (k = 0..L/2):
+//   Z[k] = X[k] + i Y[k],  Z[L-k] = conj(X[k]) + i conj(Y[k]);
+// the imaginary parts of X[0] and X[L/2] are dropped, which is the c2r
+// convention of the reference backend (ndrustfft_backend.rs:46-57).
+// Unpacking after a forward FFT:  X[k] = (Z[k] + conj Z[-k]) / 2,
+//                                 Y[k] = (Z[k] - conj Z[-k]) / (2i).
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void zpack(C2<R>* line, int L, int k, C2<R> X, C2<R> Y) {
+  if (k == 0 || 2 * k == L) {
+    line[k] = cmk<R>(X.x, Y.x);
+  } else {
+    line[k] = cmk<R>(X.x - Y.y, X.y + Y.x);
+    line[L - k] = cmk<R>(X.x + Y.y, Y.x - X.y);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void zunpack(const C2<R>* line, int L, int k, C2<R>& X, C2<R>& Y) {
+  const C2<R> z = line[k];
+  const C2<R> w = line[k == 0 ? 0 : L - k];
+  X = cmk<R>(R(0.5) * (z.x + w.x), R(0.5) * (z.y - w.y));
+  Y = cmk<R>(R(0.5) * (z.y + w.y), R(0.5) * (w.x - z.x));
+}
+
+// ---------------------------------------------------------------------------
+// P3: per (x, y) column: c2r of u and omega on the padded grid, u x omega,
+// r2c, keep iz < H.  Six real fields ride in three complex lines per column:
+//   (u_x + i u_y), (u_z + i w_x), (w_y + i w_z).
+// After the cross product the three real outputs of two columns ride in three
+// lines: (c_x0 + i c_y0), (c_x1 + i c_y1), (c_z0 + i c_z1).
+// ---------------------------------------------------------------------------
+template <typename R> struct P3Args {
+  int ncols;                        // M*M
+  const C2<R>* in; size_t fsin;     // 6 fields (M, M, H)
+  C2<R>* out; size_t fsout;         // 3 fields (M, M, H)
+};
+
+template <typename R, int M, int CP, int NT>
+__global__ void __launch_bounds__(NT) k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
+  constexpr int N = 2 * M / 3;
+  constexpr int H = N / 2 + 1;
+  constexpr int NL = 6 * CP;
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
+  const int col0 = blockIdx.x * 2 * CP;
+  // load + pack
+  for (int e = threadIdx.x; e < 2 * CP * 3 * H; e += NT) {
+    const int k = e % H;
+    const int t = (e / H) % 3;
+    const int cr = e / (3 * H);
+    const int col = col0 + cr;
+    C2<R> X = czero<R>(), Y = czero<R>();
+    if (col < a.ncols) {
+      X = a.in[(size_t)(2 * t) * a.fsin + (size_t)col * H + k];
+      Y = a.in[(size_t)(2 * t + 1) * a.fsin + (size_t)col * H + k];
+    }
+    C2<R>* line = lines + (6 * (cr / 2) + 3 * (cr % 2) + t) * M;
+    zpack<R>(line, M, k, X, Y);
+  }
+  for (int e = threadIdx.x; e < NL * (N / 2 - 1); e += NT) {
+    const int l = e / (N / 2 - 1), p = H + e % (N / 2 - 1);
+    lines[l * M + p] = czero<R>();
+  }
+  __syncthreads();
+  fft_smem<R, M, true, NT, NL, false>(lines, M, 1, tw);
+  // cross product, two phases (all reads, sync, all writes)
+  constexpr int QX = (CP * M + NT - 1) / NT;
+  C2<R> res[QX][3];
+#pragma unroll
+  for (int q = 0; q < QX; ++q) {
+    const int e = threadIdx.x + q * NT;
+    if (e < CP * M) {
+      const int pr = e / M, p = e % M;
+      R cz[2];
+#pragma unroll
+      for (int cc = 0; cc < 2; ++cc) {
+        const C2<R>* L0 = lines + (6 * pr + 3 * cc) * M;
+        const C2<R> A = L0[p], B = L0[M + p], C = L0[2 * M + p];
+        const R ux = A.x, uy = A.y, uz = B.x, wx = B.y, wy = C.x, wz = C.y;
+        res[q][cc] = cmk<R>(uy * wz - uz * wy, uz * wx - ux * wz);
+        cz[cc] = ux * wy - uy * wx;
+      }
+      res[q][2] = cmk<R>(cz[0], cz[1]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < QX; ++q) {
+    const int e = threadIdx.x + q * NT;
+    if (e < CP * M) {
+      const int pr = e / M, p = e % M;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) lines[(3 * pr + j) * M + p] = res[q][j];
+    }
+  }
+  __syncthreads();
+  fft_smem<R, M, false, NT, 3 * CP, false>(lines, M, 1, tw);
+  // unpack + store H modes of c_x, c_y, c_z for both columns of each pair
+  for (int e = threadIdx.x; e < CP * 3 * H; e += NT) {
+    const int k = e % H;
+    const int j = (e / H) % 3;
+    const int pr = e / (3 * H);
+    C2<R> X, Y;
+    zunpack<R>(lines + (3 * pr + j) * M, M, k, X, Y);
+    const int c0 = col0 + 2 * pr;
+    if (j < 2) {
+      const int col = c0 + j;
+      if (col < a.ncols) {
+        a.out[(size_t)col * H + k] = X;
+        a.out[a.fsout + (size_t)col * H + k] = Y;
+      }
+    } else {
+      if (c0 < a.ncols) a.out[2 * a.fsout + (size_t)c0 * H + k] = X;
+      if (c0 + 1 < a.ncols) a.out[2 * a.fsout + (size_t)(c0 + 1) * H + k] = Y;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// N-grid z pass: c2r of u and/or omega (already x/y-inverted and scaled by
+// 1/N^3) and max |u|^2, max |omega|^2 over the N^3 grid
+// (solver.rs:180-218 and :537-567).  Fields in: (N, N, H) x nf, order
+// u_x, u_y, u_z[, w_x, w_y, w_z].  BOTH: 6 fields -> 3 lines per column;
+// otherwise 3 fields -> lines (f0_a + i f1_a), (f0_b + i f1_b), (f2_a + i f2_b)
+// per column pair.
+// ---------------------------------------------------------------------------
+template <typename R> struct NZArgs {
+  int ncols;                     // N*N
+  const C2<R>* in; size_t fs;
+  MaxOut* out;
+  int which;                     // 1 = u only, 2 = omega only, 3 = both
+};
+
+__device__ __forceinline__ void atomic_max_pos(unsigned long long* p, double v) {
+  atomicMax(p, (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename R, int N, int CP, bool BOTH, int NT>
+__global__ void __launch_bounds__(NT) k_nz_max(NZArgs<R> a, const C2<R>* __restrict__ tw) {
+  constexpr int H = N / 2 + 1;
+  constexpr int LPP = BOTH ? 6 : 3;   // lines per column pair
+  constexpr int NL = LPP * CP;
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
+  __shared__ double red[2][32];
+  __shared__ int redn;
+  if (threadIdx.x == 0) redn = 0;
+  const int col0 = blockIdx.x * 2 * CP;
+  for (int e = threadIdx.x; e < 2 * CP * (LPP / 2) * H; e += NT) {
+    const int k = e % H;
+    const int t = (e / H) % (LPP / 2);
+    const int cr = e / ((LPP / 2) * H);
+    const int col = col0 + cr;
+    const int pr = cr / 2, cc = cr % 2;
+    C2<R> X = czero<R>(), Y = czero<R>();
+    if (BOTH) {
+      if (col < a.ncols) {
+        X = a.in[(size_t)(2 * t) * a.fs + (size_t)col * H + k];
+        Y = a.in[(size_t)(2 * t + 1) * a.fs + (size_t)col * H + k];
+      }
+      zpack<R>(lines + (6 * pr + 3 * cc + t) * N, N, k, X, Y);
+    } else {
+      // t in {0}: each column loads its f0/f1 pair; the f2 fields of the two
+      // columns of a pair share one line.
+      if (col < a.ncols) {
+        X = a.in[(size_t)col * H + k];
+        Y = a.in[a.fs + (size_t)col * H + k];
+      }
+      zpack<R>(lines + (3 * pr + cc) * N, N, k, X, Y);
+    }
+  }
+  if (!BOTH) {
+    for (int e = threadIdx.x; e < CP * H; e += NT) {
+      const int k = e % H, pr = e / H;
+      const int c0 = col0 + 2 * pr;
+      C2<R> X = czero<R>(), Y = czero<R>();
+      if (c0 < a.ncols) X = a.in[2 * a.fs + (size_t)c0 * H + k];
+      if (c0 + 1 < a.ncols) Y = a.in[2 * a.fs + (size_t)(c0 + 1) * H + k];
+      zpack<R>(lines + (3 * pr + 2) * N, N, k, X, Y);
+    }
+  }
+  __syncthreads();
+  fft_smem<R, N, true, NT, NL, false>(lines, N, 1, tw);
+  double m1 = 0.0, m2 = 0.0;
+  int bad = 0;
+  for (int e = threadIdx.x; e < CP * N; e += NT) {
+    const int pr = e / N, p = e % N;
+#pragma unroll
+    for (int cc = 0; cc < 2; ++cc) {
+      if (col0 + 2 * pr + cc >= a.ncols) continue;
+      if (BOTH) {
+        const C2<R>* L0 = lines + (6 * pr + 3 * cc) * N;
+        const C2<R> A = L0[p], B = L0[N + p], C = L0[2 * N + p];
+        const double ux = A.x, uy = A.y, uz = B.x, wx = B.y, wy = C.x, wz = C.y;
+        const double s1 = ux * ux + uy * uy + uz * uz;
+        const double s2 = wx * wx + wy * wy + wz * wz;
+        bad |= (s1 != s1) | (s2 != s2);
+        m1 = fmax(m1, s1);
+        m2 = fmax(m2, s2);
+      } else {
+        const C2<R> A = lines[(3 * pr + cc) * N + p];
+        const C2<R> Z = lines[(3 * pr + 2) * N + p];
+        const double fx = A.x, fy = A.y, fz = cc == 0 ? Z.x : Z.y;
+        const double s = fx * fx + fy * fy + fz * fz;
+        bad |= (s != s);
+        m1 = fmax(m1, s);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+  }
+  const int w = threadIdx.x / 32, ln = threadIdx.x % 32;
+  if (bad) atomicOr(&redn, 1);
+  if (ln == 0) { red[0][w] = m1; red[1][w] = m2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r1 = 0.0, r2 = 0.0;
+    for (int i = 0; i < NT / 32; ++i) { r1 = fmax(r1, red[0][i]); r2 = fmax(r2, red[1][i]); }
+    if (BOTH) {
+      atomic_max_pos(&a.out->umax2, r1);
+      atomic_max_pos(&a.out->wmax2, r2);
+    } else if (a.which == 2) {
+      atomic_max_pos(&a.out->wmax2, r1);
+    } else {
+      atomic_max_pos(&a.out->umax2, r1);
+    }
+    if (redn) atomicOr(&a.out->nan_flag, 1);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Standalone backend z passes (FftBackend::r2c_3d / c2r_3d z stage,
+// ndrustfft_backend.rs:33-57).  Real lines of length L, pairs of columns per
+// complex line.
+// ---------------------------------------------------------------------------
+template <typename R> struct FZArgs {
+  int ncols;                  // nx*ny
+  R* real; C2<R>* cplx;       // (ncols, L) real, (ncols, L/2+1) complex
+  R scale;                    // c2r: 1/(nx ny nz)
+};
+
+template <typename R, int L, int CP, int NT>
+__global__ void __launch_bounds__(NT) k_fz_r2c(FZArgs<R> a, const C2<R>* __restrict__ tw) {
+  constexpr int H = L / 2 + 1;
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
+  const int col0 = blockIdx.x * 2 * CP;
+  for (int e = threadIdx.x; e < CP * L; e += NT) {
+    const int pr = e / L, p = e % L;
+    const int c0 = col0 + 2 * pr;
+    const R x = c0 < a.ncols ? a.real[(size_t)c0 * L + p] : R(0);
+    const R y = c0 + 1 < a.ncols ? a.real[(size_t)(c0 + 1) * L + p] : R(0);
+    lines[pr * L + p] = cmk<R>(x, y);
+  }
+  __syncthreads();
+  fft_smem<R, L, false, NT, CP, false>(lines, L, 1, tw);
+  for (int e = threadIdx.x; e < CP * H; e += NT) {
+    const int pr = e / H, k = e % H;
+    const int c0 = col0 + 2 * pr;
+    C2<R> X, Y;
+    zunpack<R>(lines + pr * L, L, k, X, Y);
+    if (c0 < a.ncols) a.cplx[(size_t)c0 * H + k] = X;
+    if (c0 + 1 < a.ncols) a.cplx[(size_t)(c0 + 1) * H + k] = Y;
+  }
+}
+
+template <typename R, int L, int CP, int NT>
+__global__ void __launch_bounds__(NT) k_fz_c2r(FZArgs<R> a, const C2<R>* __restrict__ tw) {
+  constexpr int H = L / 2 + 1;
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
+  const int col0 = blockIdx.x * 2 * CP;
+  for (int e = threadIdx.x; e < CP * H; e += NT) {
+    const int pr = e / H, k = e % H;
+    const int c0 = col0 + 2 * pr;
+    const C2<R> X = c0 < a.ncols ? a.cplx[(size_t)c0 * H + k] : czero<R>();
+    const C2<R> Y = c0 + 1 < a.ncols ? a.cplx[(size_t)(c0 + 1) * H + k] : czero<R>();
+    zpack<R>(lines + pr * L, L, k, X, Y);
+  }
+  __syncthreads();
+  fft_smem<R, L, true, NT, CP, false>(lines, L, 1, tw);
+  for (int e = threadIdx.x; e < CP * L; e += NT) {
+    const int pr = e / L, p = e % L;
+    const int c0 = col0 + 2 * pr;
+    const C2<R> z = lines[pr * L + p];
+    if (c0 < a.ncols) a.real[(size_t)c0 * L + p] = z.x * a.scale;
+    if (c0 + 1 < a.ncols) a.real[(size_t)(c0 + 1) * L + p] = z.y * a.scale;
+  }
+}
+
+}  // namespace vk

@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--precision", choices=["fp64", "fp32bulk"], default="fp64",
+                    help="form of the headline run (fp32bulk only for profiling that form)")
     return ap.parse_args()
 
 
@@ -283,7 +285,7 @@ def run_ours(args, d: Dist):
     dev = d.local
     u0 = ics.von_karman_isotropic(n, kp=4.0, energy=0.5, seed=42)
     grid = vk.GridSpec(n)
-    s = vk.Periodic3D(grid, nu, u0, vk.SolverOptions(precision="fp64", device=dev))
+    s = vk.Periodic3D(grid, nu, u0, vk.SolverOptions(precision=args.precision, device=dev))
     s.step(args.warmup)
     s.dt()  # synchronise
     d.barrier()
@@ -306,7 +308,7 @@ def run_ours(args, d: Dist):
     gpu_launches = int(round(launches_per_step * args.steps)) + 2 * nspec
 
     mdl = pass_model(n)
-    elem = 16
+    elem = 16 if args.precision == "fp64" else 8
     dom = max((k for k in mdl if prof.get(k, (0, 0))[1] > 0), key=lambda k: prof[k][0])
     dom_ms = prof[dom][0] / prof[dom][1]
     hbm, hbm_src = measured_hbm()
@@ -360,7 +362,7 @@ def run_ours(args, d: Dist):
 
     # FP32-bulk form on the same workload
     fp32 = None
-    if not args.no_fp32:
+    if not args.no_fp32 and args.precision == "fp64":
         s32 = vk.Periodic3D(grid, nu, u0, vk.SolverOptions(precision="fp32bulk", device=dev))
         s32.step(args.warmup)
         s32.dt()
@@ -408,8 +410,8 @@ def run_ours(args, d: Dist):
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": d.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": n, "precision": "fp64", "replicas": d.world,
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "precision": args.precision, "replicas": d.world,
                    "l2": "no flush needed: every pass streams >= 0.9 GB (P2 writes 6x384x384x129x16 B = 1.8 GB) "
                          "through the 129 MB L2", "timing": "CUDA events on the solver stream"},
         "hbm_gbs_step": sb / (ms / args.steps * 1e-3) / 1e9,

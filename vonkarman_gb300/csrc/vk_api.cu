@@ -205,7 +205,7 @@ int cuda_fail(vk_ctx* c, cudaError_t e, const char* where) {
 
 template <typename R>
 vk::StageArgs<R> stage_args(vk_ctx* c, int op, void* out) {
-  vk::StageArgs<R> s;
+  vk::StageArgs<R> s{};
   s.op = op;
   s.cs = c->cs;
   s.u = (C2<R>*)c->u;
@@ -221,7 +221,7 @@ vk::StageArgs<R> stage_args(vk_ctx* c, int op, void* out) {
 
 template <typename R>
 cudaError_t nle_t(vk_ctx* c, const void* in, int op, void* out) {
-  vk::NleParams<R> p;
+  vk::NleParams<R> p{};
   p.N = c->N;
   p.ks = c->ks;
   p.in = (const C2<R>*)in;
@@ -240,7 +240,7 @@ cudaError_t nle(vk_ctx* c, const void* in, int op, void* out = nullptr) {
 
 template <typename R>
 cudaError_t ngrid_t(vk_ctx* c, const void* in, int which) {
-  vk::NgridParams<R> p;
+  vk::NgridParams<R> p{};
   p.N = c->N;
   p.ks = c->ks;
   p.in = (const C2<R>*)in;
@@ -870,7 +870,7 @@ const char* vk_fft_last_error(const vk_fft* p) { return p ? p->err.c_str() : g_c
 
 template <typename R>
 static cudaError_t fft_exec(vk_fft* p, bool forward, void* real, void* cplx, cudaStream_t s) {
-  vk::FftParams<R> f;
+  vk::FftParams<R> f{};
   f.nx = p->nx; f.ny = p->ny; f.nz = p->nz;
   f.real = (R*)real;
   f.cplx = (C2<R>*)cplx;

@@ -184,6 +184,24 @@ def step_bytes(n: int, elem: int) -> float:
     return per * elem
 
 
+# DRAM traffic (read + write bytes) of one launch from the committed ncu
+# captures (profiles/k_p3_*_isotropic_n128.md), taken at N=128 and scaled to a
+# full launch at grid n by the number of padded columns x modes (M^2 H).
+NCU_TRAFFIC = {
+    ("P3_z_c2r_cross_r2c", "fp64"): (128, 230115840 + 85875200),
+    ("P3_z_c2r_cross_r2c", "fp32bulk"): (128, 115037952 + 29144576),
+}
+
+
+def scaled_traffic(kernel: str, precision: str, n: int):
+    hit = NCU_TRAFFIC.get((kernel, precision))
+    if not hit:
+        return None
+    n0, b0 = hit
+    m, m0 = 3 * n // 2, 3 * n0 // 2
+    return b0 * (m * m * (n // 2 + 1)) / (m0 * m0 * (n0 // 2 + 1))
+
+
 def measured_hbm():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -416,7 +434,9 @@ def run_ours(args, d: Dist):
                          "through the 129 MB L2", "timing": "CUDA events on the solver stream"},
         "hbm_gbs_step": sb / (ms / args.steps * 1e-3) / 1e9,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_source": hbm_src,
+                     "frac": achieved / hbm, "traffic": scaled_traffic(dom, args.precision, n),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at N=128, scaled by M^2 H",
+                     "peak_source": hbm_src,
                      "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
         "fp64_roofline": {"kernel": dom, "achieved": dom_gflops, "peak": fp64_peak, "unit": "GFLOP/s",
                           "frac": dom_gflops / fp64_peak, "peak_source": "measured live (FP64 FMA probe)",

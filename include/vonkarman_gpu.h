@@ -188,6 +188,32 @@ int vk_event_elapsed(vk_ctx* ctx, int32_t a, int32_t b, double* ms);
 int vk_pinned_alloc(size_t bytes, void** out);
 int vk_pinned_free(void* p);
 
+/* --- allocation-free entry point (no counterpart in the reference: its
+ *     energy_spectrum, vonkarman-diag/src/spectrum.rs:13-60, works on host
+ *     arrays) ------------------------------------------------------------- */
+/* Shell spectrum E(k) of a state the caller already holds in device memory,
+ * for callers that must not allocate device memory: code recording a CUDA
+ * graph, code under a framework's caching allocator that owns all device
+ * memory, latency-critical loops that cannot take an allocation's implicit
+ * synchronisation.  Nothing is allocated: the scratch is a fixed 896 KiB
+ * device array inside the library, held on every GPU that loads it until the
+ * process exits, which limits n to 512 (at most 448 shells).
+ *   u_hat        three contiguous components (n, n, n/2+1) on the current
+ *                device, double2 (precision VK_PRECISION_FP64) or float2
+ *                (VK_PRECISION_FP32BULK)
+ *   spectrum_out ceil(sqrt(3)*n/2)+1 doubles on the device (spectrum[i] =
+ *                E(shell i), conventions of energy_spectrum)
+ *   stream       cudaStream_t to enqueue on (NULL = default stream); the call
+ *                returns without synchronising.
+ * The first call on each device looks up the scratch address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one scratch array: calls that overlap on the GPU (other
+ * streams, concurrently launched graphs) race and must be serialised by the
+ * caller.  Errors: VK_ERR_INVALID / VK_ERR_UNSUPPORTED (n > 512), message in
+ * vk_last_error(NULL). */
+int vk_spectrum_noalloc(const void* u_hat, int32_t n, double l, int32_t precision, double* spectrum_out,
+                        void* stream);
+
 /* --- FFT backend (replaces FftBackend<f64>, vonkarman-fft/src/backend.rs:9-25,
  *     and create_backend, vonkarman-fft/src/select.rs:34-67) ------------------- */
 /* Each of nx, ny, nz in {8,16,...,512} or {12,24,...,768}. */

@@ -80,6 +80,7 @@ SIGNATURES = {
     "vk_event_elapsed": (c_int, [_CTX, c_int32, c_int32, _DP]),
     "vk_pinned_alloc": (c_int, [ctypes.c_size_t, POINTER(c_void_p)]),
     "vk_pinned_free": (c_int, [c_void_p]),
+    "vk_spectrum_noalloc": (c_int, [c_void_p, c_int32, c_double, c_int32, c_void_p, c_void_p]),
     "vk_fft_create": (c_int, [c_int32, c_int32, c_int32, c_int32, c_int32, POINTER(c_void_p)]),
     "vk_fft_destroy": (c_int, [c_void_p]),
     "vk_fft_last_error": (c_char_p, [c_void_p]),

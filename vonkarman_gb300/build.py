@@ -1,6 +1,6 @@
 """Builds libvonkarman_gpu.so in-tree with nvcc for sm_103a.
 
-The four translation units compile in parallel; the shared library links the
+The translation units compile in parallel; the shared library links the
 CUDA runtime statically, so it has no dependency besides the driver.
 """
 
@@ -19,7 +19,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libvonkarman_gpu.so")
 
-SOURCES = ["vk_engine_f64.cu", "vk_engine_f32.cu", "vk_misc.cu", "vk_api.cu"]
+SOURCES = ["vk_engine_f64.cu", "vk_engine_f32.cu", "vk_misc.cu", "vk_api.cu", "vk_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
 

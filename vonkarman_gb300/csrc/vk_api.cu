@@ -403,6 +403,11 @@ void free_ctx(vk_ctx* c) {
 
 }  // namespace
 
+namespace vk {
+// Error message of a context-free entry point, read back by vk_last_error(NULL).
+void set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
+}  // namespace vk
+
 // ============================================================================
 extern "C" {
 

@@ -66,7 +66,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   // P3
   {
     TimerScope ts(p.timer, PASS_P3, s);
-    constexpr int CP = zpairs<M, 768>();
+    constexpr int CP = zpairs<M, 384>();
     constexpr int NT = zthreads<6 * CP, M>();
     const size_t smem = (size_t)6 * CP * M * sizeof(C2<R>);
     constexpr auto kern = k_p3<R, M, CP, NT>;

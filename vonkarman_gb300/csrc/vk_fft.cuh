@@ -78,78 +78,151 @@ __host__ __device__ constexpr int plan_radix(int L, int s) {
 __host__ __device__ constexpr bool fft_len_supported(int L) { return plan_stages(L) > 0; }
 
 // ---------------------------------------------------------------------------
-// Radix kernels (in registers).  INV selects exp(+i...).
+// Radix kernels (in registers), with the stage twiddles fused into the first
+// butterfly layer: a + w b costs 4 FMAs and a - w b = 2a - (a + w b) costs 2,
+// instead of a complex multiply (4) plus two complex adds (4).  INV selects
+// exp(+i...) and conjugated twiddles.  TW = false: first stage, no twiddles.
 // ---------------------------------------------------------------------------
 template <typename R, bool INV>
-__device__ __forceinline__ void dft2(C2<R>* v) {
-  C2<R> a = v[0], b = v[1];
-  v[0] = cadd<R>(a, b);
-  v[1] = csub<R>(a, b);
+__device__ __forceinline__ C2<R> tw_mul(C2<R> w, C2<R> b) {  // w b (conj(w) b if INV)
+  return INV ? cmk<R>(fma(w.x, b.x, w.y * b.y), fma(w.x, b.y, -(w.y * b.x)))
+             : cmk<R>(fma(w.x, b.x, -(w.y * b.y)), fma(w.x, b.y, w.y * b.x));
+}
+template <typename R, bool INV>
+__device__ __forceinline__ C2<R> tw_fma(C2<R> a, C2<R> w, C2<R> b) {  // a + w b (a + conj(w) b if INV)
+  return INV ? cmk<R>(fma(w.y, b.y, fma(w.x, b.x, a.x)), fma(-w.y, b.x, fma(w.x, b.y, a.y)))
+             : cmk<R>(fma(-w.y, b.y, fma(w.x, b.x, a.x)), fma(w.y, b.x, fma(w.x, b.y, a.y)));
+}
+template <typename R>
+__device__ __forceinline__ C2<R> twice_minus(C2<R> a, C2<R> t) {  // 2a - t
+  return cmk<R>(fma(R(2), a.x, -t.x), fma(R(2), a.y, -t.y));
+}
+// multiply by -i (forward) or +i (inverse)
+template <typename R, bool INV>
+__device__ __forceinline__ C2<R> rot(C2<R> a) { return INV ? cmul_i<R>(a) : cmul_mi<R>(a); }
+
+// (s, d) pair: a + (x, y) and a - (x, y)
+template <typename R>
+__device__ __forceinline__ void bfly(C2<R> a, C2<R> b, C2<R>& p, C2<R>& m) {
+  p = cadd<R>(a, b);
+  m = csub<R>(a, b);
 }
 
-template <typename R, bool INV>
-__device__ __forceinline__ void dft4(C2<R>& a0, C2<R>& a1, C2<R>& a2, C2<R>& a3) {
-  C2<R> t0 = cadd<R>(a0, a2), t1 = csub<R>(a0, a2);
-  C2<R> t2 = cadd<R>(a1, a3), t3 = csub<R>(a1, a3);
-  t3 = INV ? cmul_i<R>(t3) : cmul_mi<R>(t3);
-  a0 = cadd<R>(t0, t2);
-  a2 = csub<R>(t0, t2);
-  a1 = cadd<R>(t1, t3);
-  a3 = csub<R>(t1, t3);
-}
-
-template <typename R, bool INV>
-__device__ __forceinline__ void dft3(C2<R>* v) {
-  const R c = R(0.86602540378443864676372317075293618);  // sqrt(3)/2
-  C2<R> a0 = v[0], a1 = v[1], a2 = v[2];
-  C2<R> t = cadd<R>(a1, a2);
-  C2<R> d = csub<R>(a1, a2);
-  C2<R> m = cmk<R>(a0.x - R(0.5) * t.x, a0.y - R(0.5) * t.y);
-  // forward: d * (-i c); inverse: d * (+i c)
-  C2<R> e = INV ? cmk<R>(-c * d.y, c * d.x) : cmk<R>(c * d.y, -c * d.x);
-  v[0] = cadd<R>(a0, t);
-  v[1] = cadd<R>(m, e);
-  v[2] = csub<R>(m, e);
-}
-
-template <typename R, bool INV>
-__device__ __forceinline__ void dft8(C2<R>* v) {
-  const R h = R(0.70710678118654752440084436210484904);  // sqrt(2)/2
-  C2<R> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
-  C2<R> o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
-  dft4<R, INV>(e0, e1, e2, e3);
-  dft4<R, INV>(o0, o1, o2, o3);
-  // o_q *= W8^q  (forward W8 = h(1 - i), inverse h(1 + i))
-  C2<R> w1, w3;
-  if (INV) {
-    w1 = cmk<R>(h * (o1.x - o1.y), h * (o1.x + o1.y));
-    w3 = cmk<R>(-h * (o3.x + o3.y), h * (o3.x - o3.y));
-    o2 = cmul_i<R>(o2);
+// radix-2: v[1] carries twiddle w[1]
+template <typename R, bool INV, bool TW>
+__device__ __forceinline__ void rad2(C2<R>* v, const C2<R>* w) {
+  C2<R> p, m;
+  if (TW) {
+    p = tw_fma<R, INV>(v[0], w[1], v[1]);
+    m = twice_minus<R>(v[0], p);
   } else {
-    w1 = cmk<R>(h * (o1.x + o1.y), h * (o1.y - o1.x));
-    w3 = cmk<R>(h * (o3.y - o3.x), -h * (o3.x + o3.y));
-    o2 = cmul_mi<R>(o2);
+    bfly<R>(v[0], v[1], p, m);
   }
-  v[0] = cadd<R>(e0, o0);
-  v[4] = csub<R>(e0, o0);
-  v[1] = cadd<R>(e1, w1);
-  v[5] = csub<R>(e1, w1);
-  v[2] = cadd<R>(e2, o2);
-  v[6] = csub<R>(e2, o2);
-  v[3] = cadd<R>(e3, w3);
-  v[7] = csub<R>(e3, w3);
+  v[0] = p;
+  v[1] = m;
 }
 
-template <typename R, bool INV, int RAD>
-__device__ __forceinline__ void dft(C2<R>* v) {
-  if constexpr (RAD == 8) {
-    dft8<R, INV>(v);
-  } else if constexpr (RAD == 4) {
-    dft4<R, INV>(v[0], v[1], v[2], v[3]);
-  } else if constexpr (RAD == 3) {
-    dft3<R, INV>(v);
+// 4-point DFT of (a0, w_a a1, w_b a2, w_c a3) where the pairs (a0, a2) and
+// (a1, a3) form the first butterfly layer.  Outputs in natural order.
+template <typename R, bool INV, bool TW>
+__device__ __forceinline__ void rad4_core(C2<R> a0, C2<R> a1, C2<R> a2, C2<R> a3, C2<R> w1, C2<R> w2, C2<R> w3,
+                                          C2<R>& y0, C2<R>& y1, C2<R>& y2, C2<R>& y3) {
+  C2<R> t0, t1, t2, t3;
+  if (TW) {
+    t0 = tw_fma<R, INV>(a0, w2, a2);
+    t1 = twice_minus<R>(a0, t0);
+    const C2<R> b1 = tw_mul<R, INV>(w1, a1);
+    t2 = tw_fma<R, INV>(b1, w3, a3);
+    t3 = twice_minus<R>(b1, t2);
   } else {
-    dft2<R, INV>(v);
+    bfly<R>(a0, a2, t0, t1);
+    bfly<R>(a1, a3, t2, t3);
+  }
+  t3 = rot<R, INV>(t3);
+  bfly<R>(t0, t2, y0, y2);
+  bfly<R>(t1, t3, y1, y3);
+}
+
+template <typename R, bool INV, bool TW>
+__device__ __forceinline__ void rad4(C2<R>* v, const C2<R>* w) {
+  rad4_core<R, INV, TW>(v[0], v[1], v[2], v[3], w[1], w[2], w[3], v[0], v[1], v[2], v[3]);
+}
+
+template <typename R, bool INV, bool TW>
+__device__ __forceinline__ void rad3(C2<R>* v, const C2<R>* w) {
+  const R c = R(0.86602540378443864676372317075293618);  // sqrt(3)/2
+  C2<R> t, d;
+  if (TW) {
+    const C2<R> b1 = tw_mul<R, INV>(w[1], v[1]);
+    t = tw_fma<R, INV>(b1, w[2], v[2]);   // v1 + v2
+    d = twice_minus<R>(b1, t);            // v1 - v2
+  } else {
+    bfly<R>(v[1], v[2], t, d);
+  }
+  const C2<R> a0 = v[0];
+  const C2<R> m = cmk<R>(fma(R(-0.5), t.x, a0.x), fma(R(-0.5), t.y, a0.y));
+  v[0] = cadd<R>(a0, t);
+  if (INV) {
+    v[1] = cmk<R>(fma(-c, d.y, m.x), fma(c, d.x, m.y));
+    v[2] = cmk<R>(fma(c, d.y, m.x), fma(-c, d.x, m.y));
+  } else {
+    v[1] = cmk<R>(fma(c, d.y, m.x), fma(-c, d.x, m.y));
+    v[2] = cmk<R>(fma(-c, d.y, m.x), fma(c, d.x, m.y));
+  }
+}
+
+// radix-8 = two 4-point DFTs (even / odd inputs) and a W8 layer.
+template <typename R, bool INV, bool TW>
+__device__ __forceinline__ void rad8(C2<R>* v, const C2<R>* w) {
+  const R h = R(0.70710678118654752440084436210484904);  // sqrt(2)/2
+  const C2<R> one = cmk<R>(R(1), R(0));
+  C2<R> e0, e1, e2, e3, o0, o1, o2, o3;
+  // even inputs v0, v2, v4, v6 (twiddles w0 = 1, w2, w4, w6)
+  rad4_core<R, INV, TW>(v[0], v[2], v[4], v[6], TW ? w[2] : one, TW ? w[4] : one, TW ? w[6] : one,
+                        e0, e1, e2, e3);
+  // odd inputs v1, v3, v5, v7: fold w1 into the first pair's base
+  if (TW) {
+    const C2<R> b1 = tw_mul<R, INV>(w[1], v[1]);
+    const C2<R> b3 = tw_mul<R, INV>(w[3], v[3]);
+    C2<R> t0 = tw_fma<R, INV>(b1, w[5], v[5]);
+    C2<R> t1 = twice_minus<R>(b1, t0);
+    C2<R> t2 = tw_fma<R, INV>(b3, w[7], v[7]);
+    C2<R> t3 = twice_minus<R>(b3, t2);
+    t3 = rot<R, INV>(t3);
+    bfly<R>(t0, t2, o0, o2);
+    bfly<R>(t1, t3, o1, o3);
+  } else {
+    rad4_core<R, INV, false>(v[1], v[3], v[5], v[7], one, one, one, o0, o1, o2, o3);
+  }
+  // W8 layer
+  bfly<R>(e0, o0, v[0], v[4]);
+  const C2<R> r2 = rot<R, INV>(o2);
+  bfly<R>(e2, r2, v[2], v[6]);
+  // W8^1 o1 = h (s + i d)
+  R s1, d1, s3, d3;
+  if (INV) {
+    s1 = o1.x - o1.y; d1 = o1.x + o1.y;
+    s3 = -(o3.x + o3.y); d3 = o3.x - o3.y;
+  } else {
+    s1 = o1.x + o1.y; d1 = o1.y - o1.x;
+    s3 = o3.y - o3.x; d3 = -(o3.x + o3.y);
+  }
+  v[1] = cmk<R>(fma(h, s1, e1.x), fma(h, d1, e1.y));
+  v[5] = cmk<R>(fma(-h, s1, e1.x), fma(-h, d1, e1.y));
+  v[3] = cmk<R>(fma(h, s3, e3.x), fma(h, d3, e3.y));
+  v[7] = cmk<R>(fma(-h, s3, e3.x), fma(-h, d3, e3.y));
+}
+
+template <typename R, bool INV, int RAD, bool TW>
+__device__ __forceinline__ void dft(C2<R>* v, const C2<R>* w) {
+  if constexpr (RAD == 8) {
+    rad8<R, INV, TW>(v, w);
+  } else if constexpr (RAD == 4) {
+    rad4<R, INV, TW>(v, w);
+  } else if constexpr (RAD == 3) {
+    rad3<R, INV, TW>(v, w);
+  } else {
+    rad2<R, INV, TW>(v, w);
   }
 }
 
@@ -188,14 +261,12 @@ struct StockhamStage {
         const int l = LINE_FAST ? (g % NLINES) : (g / NB);
         const int j = LINE_FAST ? (g / NLINES) : (g % NB);
         const int k = j % NS;
+        C2<R> w[RAD];
         if (S > 0) {
 #pragma unroll
-          for (int r = 1; r < RAD; ++r) {
-            const C2<R> w = tw[r * k * TWS];
-            v[q][r] = INV ? cmulc<R>(v[q][r], w) : cmul<R>(v[q][r], w);
-          }
+          for (int r = 1; r < RAD; ++r) w[r] = tw[r * k * TWS];
         }
-        dft<R, INV, RAD>(v[q]);
+        dft<R, INV, RAD, (S > 0)>(v[q], w);
         C2<R>* dst = buf + l * ld_line;
         const int base = (j - k) * RAD + k;
 #pragma unroll

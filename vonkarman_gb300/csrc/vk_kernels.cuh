@@ -54,13 +54,16 @@ __host__ __device__ constexpr int strided_threads() {
 template <int L, int TARGET> __host__ __device__ constexpr int zpairs() { return cmax(1, TARGET / L); }
 template <int NLINES, int L>
 __host__ __device__ constexpr int zthreads() { return cmax(64, cmin(1024, round32(NLINES * L / 8))); }
+// Minimum resident CTAs per SM requested from the compiler: enough for 24
+// warps per SM, which caps registers near 85 per thread.
+template <int NT> __host__ __device__ constexpr int min_blocks() { return cmax(1, 768 / NT); }
 
 // ---------------------------------------------------------------------------
 // Generic strided pass: one field of TZ interleaved lines per CTA.
 // blockIdx.x = f + nfields * (ztile + nztiles * outer)
 // ---------------------------------------------------------------------------
 template <typename R, int L, bool INV, int TZ, int NT, class Op>
-__global__ void __launch_bounds__(NT) k_strided(Op op, const C2<R>* __restrict__ tw) {
+__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_strided(Op op, const C2<R>* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* buf = reinterpret_cast<C2<R>*>(vk_smem);
   const int f = blockIdx.x % op.nfields;
@@ -302,7 +305,7 @@ template <typename R> struct P5Args {
 };
 
 template <typename R, int L, int TZ, int NT>
-__global__ void __launch_bounds__(NT) k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
+__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int N = 2 * L / 3;
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* buf = reinterpret_cast<C2<R>*>(vk_smem);
@@ -392,7 +395,7 @@ template <typename R> struct P3Args {
 };
 
 template <typename R, int M, int CP, int NT>
-__global__ void __launch_bounds__(NT) k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
+__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int N = 2 * M / 3;
   constexpr int H = N / 2 + 1;
   constexpr int NL = 6 * CP;
@@ -492,7 +495,7 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long* p, double v) 
 }
 
 template <typename R, int N, int CP, bool BOTH, int NT>
-__global__ void __launch_bounds__(NT) k_nz_max(NZArgs<R> a, const C2<R>* __restrict__ tw) {
+__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_nz_max(NZArgs<R> a, const C2<R>* __restrict__ tw) {
   constexpr int H = N / 2 + 1;
   constexpr int LPP = BOTH ? 6 : 3;   // lines per column pair
   constexpr int NL = LPP * CP;
@@ -598,7 +601,7 @@ template <typename R> struct FZArgs {
 };
 
 template <typename R, int L, int CP, int NT>
-__global__ void __launch_bounds__(NT) k_fz_r2c(FZArgs<R> a, const C2<R>* __restrict__ tw) {
+__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_fz_r2c(FZArgs<R> a, const C2<R>* __restrict__ tw) {
   constexpr int H = L / 2 + 1;
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
@@ -623,7 +626,7 @@ __global__ void __launch_bounds__(NT) k_fz_r2c(FZArgs<R> a, const C2<R>* __restr
 }
 
 template <typename R, int L, int CP, int NT>
-__global__ void __launch_bounds__(NT) k_fz_c2r(FZArgs<R> a, const C2<R>* __restrict__ tw) {
+__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_fz_c2r(FZArgs<R> a, const C2<R>* __restrict__ tw) {
   constexpr int H = L / 2 + 1;
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);

@@ -165,6 +165,26 @@ int vk_spectrum(vk_ctx* ctx, double* shells, double* spectrum, int32_t n);
 int vk_nonlinear_host(vk_ctx* ctx, const double* ux, const double* uy, const double* uz, double* nx_out,
                       double* ny_out, double* nz_out);
 
+/* --- discrete adjoint (no reference counterpart: the reference has no
+ *     adjoint; the forward map it differentiates is Domain::step with the
+ *     reference ETD-RK4 stages, solver.rs:221-400) --------------------------- */
+/* Autograd-Function forward: runs nsteps steps (dt_mode must be fixed) from the
+ * current state, keeping nsnap level-1 checkpoints (one every
+ * ceil(nsteps/nsnap) steps), and returns J = enstrophy of the final state
+ * (the reference convention, solver.rs:436-465).  The state advances. */
+int vk_adjoint_forward(vk_ctx* ctx, int64_t nsteps, int32_t nsnap, double* J);
+/* Autograd-Function backward: dJ/du_0 for the last vk_adjoint_forward, in the
+ * L2 inner product of the physical fields (<a,b> = sum w Re(a conj b) / N^6),
+ * projected onto real, divergence-free fields with zero Nyquist entries.
+ * Segments are recomputed from their checkpoint storing u, a, b, c of every
+ * step (4 ceil(nsteps/nsnap) + 1 states), then reversed. */
+int vk_adjoint_backward(vk_ctx* ctx, double* gx, double* gy, double* gz);
+/* Transpose of compute_nonlinear's linearisation at x applied to nbar (raw
+ * Euclidean inner product of the stored entries), on host arrays. */
+int vk_nonlinear_adjoint_host(vk_ctx* ctx, const double* ux, const double* uy, const double* uz,
+                              const double* bx, const double* by, const double* bz, double* ox, double* oy,
+                              double* oz);
+
 /* --- measurement (no reference counterpart: the reference has no profiler
  *     hook beyond its total wall time, vonkarman-bin/src/run.rs:73,200) ----- */
 /* vk_step with CUDA events recorded on the context's stream around the
@@ -172,7 +192,7 @@ int vk_nonlinear_host(vk_ctx* ctx, const double* ux, const double* uy, const dou
 int vk_step_timed(vk_ctx* ctx, int64_t nsteps, double* elapsed_ms);
 /* Per-pass CUDA-event timing of every launch while enabled (see
  * vk_profile_pass_name for the pass ids; VK_NPASS passes). */
-#define VK_NPASS 15
+#define VK_NPASS 20
 int vk_profile_enable(vk_ctx* ctx, int32_t enable);
 int vk_profile_read(vk_ctx* ctx, double* ms, int64_t* launches, int32_t n);
 const char* vk_profile_pass_name(int32_t id);

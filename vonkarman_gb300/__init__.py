@@ -18,9 +18,11 @@ from .solver import (  # noqa: F401
     create_backend,
     dissipation_spectrum,
     energy_spectrum,
+    l2_inner,
+    nonlinear_adjoint,
 )
 from . import ics  # noqa: F401
 
 __all__ = ["GridSpec", "GpuFftBackend", "Periodic3D", "ScalarDiagnostics", "SolverOptions",
            "compensated_spectrum", "compute_nonlinear", "create_backend", "dissipation_spectrum",
-           "energy_spectrum", "ics"]
+           "energy_spectrum", "ics", "l2_inner", "nonlinear_adjoint"]

@@ -13,7 +13,7 @@ from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_uint6
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "libvonkarman_gpu.so")
 ABI_VERSION = 1
-NPASS = 15
+NPASS = 20
 
 VK_OK = 0
 STATUS_NAMES = {0: "VK_OK", 1: "VK_ERR_INVALID", 2: "VK_ERR_UNSUPPORTED", 3: "VK_ERR_CUDA",
@@ -70,6 +70,9 @@ SIGNATURES = {
     "vk_spectrum_len": (c_int, [_CTX, POINTER(c_int32)]),
     "vk_spectrum": (c_int, [_CTX, _DP, _DP, c_int32]),
     "vk_nonlinear_host": (c_int, [_CTX, _DP, _DP, _DP, _DP, _DP, _DP]),
+    "vk_adjoint_forward": (c_int, [_CTX, c_int64, c_int32, _DP]),
+    "vk_adjoint_backward": (c_int, [_CTX, _DP, _DP, _DP]),
+    "vk_nonlinear_adjoint_host": (c_int, [_CTX, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),
     "vk_step_timed": (c_int, [_CTX, c_int64, _DP]),
     "vk_profile_enable": (c_int, [_CTX, c_int32]),
     "vk_profile_read": (c_int, [_CTX, _DP, POINTER(c_int64), c_int32]),

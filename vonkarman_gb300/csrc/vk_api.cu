@@ -165,6 +165,23 @@ struct vk_ctx {
   double ks = 1.0;
   vk::ContourConsts cc{};
   EventTimer* prof = nullptr;
+  // discrete adjoint (allocated on first use)
+  struct Adjoint {
+    int64_t nsteps = 0;
+    int64_t K = 0;                  // steps per checkpoint segment
+    int64_t nseg = 0;
+    std::vector<void*> ckpt;        // state at the start of each segment
+    std::vector<void*> seg;         // S[0..K], A[0..K-1], B[0..K-1], C[0..K-1]
+    void* ub = nullptr;
+    void* acc = nullptr;
+    void* nb = nullptr;
+    void* n1b = nullptr;
+    void* bufA = nullptr;
+    void* bufB = nullptr;
+    size_t bufA_bytes = 0, bufB_bytes = 0;
+    bool ready = false;
+    double J = 0.0;
+  } adj;
   cudaEvent_t tev[2] = {nullptr, nullptr};
   cudaEvent_t marks[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   std::string err;
@@ -213,6 +230,7 @@ vk::StageArgs<R> stage_args(vk_ctx* c, int op, void* out) {
   s.n1 = (C2<R>*)c->n1;
   s.acc = (C2<R>*)c->acc;
   s.out = (C2<R>*)out;
+  s.u_out = s.u;
   s.etd = c->etd;
   s.dt = &c->dsc->dt;
   s.nu = c->cfg.nu;
@@ -387,7 +405,21 @@ int download_state(vk_ctx* c, const void* srcdev, double* ux, double* uy, double
   return VK_OK;
 }
 
+void free_adjoint(vk_ctx* c) {
+  for (void* p : c->adj.ckpt)
+    if (p) cudaFree(p);
+  for (void* p : c->adj.seg)
+    if (p) cudaFree(p);
+  c->adj.ckpt.clear();
+  c->adj.seg.clear();
+  void* ptrs[] = {c->adj.ub, c->adj.acc, c->adj.nb, c->adj.n1b, c->adj.bufA, c->adj.bufB};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  c->adj = vk_ctx::Adjoint();
+}
+
 void free_ctx(vk_ctx* c) {
+  free_adjoint(c);
   delete c->prof;
   c->prof = nullptr;
   for (cudaEvent_t& e : c->tev)
@@ -717,6 +749,219 @@ int vk_nonlinear_host(vk_ctx* c, const double* ux, const double* uy, const doubl
   return download_state(c, c->n1, ox, oy, oz);
 }
 
+}  // extern "C"
+
+namespace {
+
+size_t state_bytes(const vk_ctx* c) { return 3 * c->cs * c->esz; }
+
+cudaError_t adj_alloc(vk_ctx* c, int64_t nseg, int64_t K) {
+  auto& a = c->adj;
+  const size_t sb = state_bytes(c);
+  cudaError_t e;
+  if ((int64_t)a.ckpt.size() != nseg || (int64_t)a.seg.size() != 4 * K + 1) {
+    for (void* p : a.ckpt)
+      if (p) cudaFree(p);
+    for (void* p : a.seg)
+      if (p) cudaFree(p);
+    a.ckpt.assign((size_t)nseg, nullptr);
+    a.seg.assign((size_t)(4 * K + 1), nullptr);
+    for (auto& p : a.ckpt)
+      if ((e = cudaMalloc(&p, sb)) != cudaSuccess) return e;
+    for (auto& p : a.seg)
+      if ((e = cudaMalloc(&p, sb)) != cudaSuccess) return e;
+  }
+  void** st[] = {&a.ub, &a.acc, &a.nb, &a.n1b};
+  for (void** p : st)
+    if (!*p && (e = cudaMalloc(p, sb)) != cudaSuccess) return e;
+  const size_t N = c->N, H = c->H, M = c->M;
+  const size_t ab = std::max(8 * M * N * H, 6 * M * M * H) * c->esz;
+  const size_t bb = std::max(9 * M * M * H, 6 * M * N * H) * c->esz;
+  if (!a.bufA && (e = cudaMalloc(&a.bufA, ab)) != cudaSuccess) return e;
+  if (!a.bufB && (e = cudaMalloc(&a.bufB, bb)) != cudaSuccess) return e;
+  a.bufA_bytes = ab;
+  a.bufB_bytes = bb;
+  a.K = K;
+  a.nseg = nseg;
+  return cudaSuccess;
+}
+
+// One forward stage NLE with explicit state pointers (recompute of a, b, c).
+template <typename R>
+cudaError_t nle_stage_t(vk_ctx* c, const void* in, int op, void* u, void* temp, void* u_out) {
+  vk::NleParams<R> p{};
+  p.N = c->N;
+  p.ks = c->ks;
+  p.in = (const C2<R>*)in;
+  p.cs = c->cs;
+  p.bufA = (C2<R>*)c->bufA;
+  p.bufB = (C2<R>*)c->bufB;
+  p.twM = (const C2<R>*)c->twM;
+  p.st = stage_args<R>(c, op, nullptr);
+  p.st.u = (C2<R>*)u;
+  p.st.temp = (C2<R>*)temp;
+  p.st.u_out = (C2<R>*)u_out;
+  p.timer = c->prof;
+  return vk::Engine<R>::nle(p, c->stream);
+}
+
+cudaError_t nle_stage(vk_ctx* c, const void* in, int op, void* u, void* temp, void* u_out) {
+  return c->fp32 ? nle_stage_t<float>(c, in, op, u, temp, u_out) : nle_stage_t<double>(c, in, op, u, temp, u_out);
+}
+
+template <typename R>
+cudaError_t nla_t(vk_ctx* c, const void* x, const void* nbsrc, int slot, int op, void* out) {
+  auto& a = c->adj;
+  vk::NlaParams<R> p{};
+  p.N = c->N;
+  p.ks = c->ks;
+  p.x = (const C2<R>*)x;
+  p.cs = c->cs;
+  p.nb = (const C2<R>*)nbsrc;
+  p.etd = c->etd;
+  p.slot = slot;
+  p.fac = 1.0;
+  p.dt = &c->dsc->dt;
+  p.bufA = (C2<R>*)a.bufA;
+  p.bufB = (C2<R>*)a.bufB;
+  p.twM = (const C2<R>*)c->twM;
+  p.st.op = op;
+  p.st.cs = c->cs;
+  p.st.ub = (C2<R>*)a.ub;
+  p.st.acc = (C2<R>*)a.acc;
+  p.st.nb = (C2<R>*)a.nb;
+  p.st.n1b = (C2<R>*)a.n1b;
+  p.st.out = (C2<R>*)out;
+  p.st.etd = c->etd;
+  p.st.dt = &c->dsc->dt;
+  p.timer = c->prof;
+  return vk::Engine<R>::nle_adjoint(p, c->stream);
+}
+
+cudaError_t nla(vk_ctx* c, const void* x, const void* nbsrc, int slot, int op, void* out = nullptr) {
+  return c->fp32 ? nla_t<float>(c, x, nbsrc, slot, op, out) : nla_t<double>(c, x, nbsrc, slot, op, out);
+}
+
+cudaError_t adj_mode(vk_ctx* c, const void* in, void* out, int mode) {
+  return c->fp32 ? vk::Engine<float>::adj_mode(c->N, c->ks, c->cs, (const float2*)in, (float2*)out, mode, c->stream)
+                 : vk::Engine<double>::adj_mode(c->N, c->ks, c->cs, (const double2*)in, (double2*)out, mode,
+                                                c->stream);
+}
+
+cudaError_t herm_avg(vk_ctx* c, const void* in, void* out) {
+  return c->fp32 ? vk::Engine<float>::hermitian_avg(c->N, c->cs, (const float2*)in, (float2*)out, c->stream)
+                 : vk::Engine<double>::hermitian_avg(c->N, c->cs, (const double2*)in, (double2*)out, c->stream);
+}
+
+// Adjoint of one reference-variant ETD-RK4 step (solver.rs:221-379 transposed)
+// taken from S with stage inputs A = a, B = b, C = c; ub is updated in place.
+cudaError_t adjoint_step(vk_ctx* c, void* S, void* A, void* B, void* C) {
+  auto& a = c->adj;
+  cudaError_t e;
+  if ((e = nla(c, C, a.ub, vk::E_B4, vk::ADJ_C)) != cudaSuccess) return e;
+  if ((e = nla(c, B, a.nb, -1, vk::ADJ_B)) != cudaSuccess) return e;
+  if ((e = nla(c, A, a.nb, -1, vk::ADJ_A)) != cudaSuccess) return e;
+  return nla(c, S, a.n1b, -1, vk::ADJ_U);
+}
+
+// Forward step from S storing the stage inputs A, B, C and the next state in Snext.
+cudaError_t forward_step_store(vk_ctx* c, void* S, void* A, void* B, void* C, void* Snext) {
+  cudaError_t e;
+  if ((e = nle_stage(c, S, vk::ST_ETD_REF_1, S, A, S)) != cudaSuccess) return e;
+  if ((e = nle_stage(c, A, vk::ST_ETD_REF_2, S, B, S)) != cudaSuccess) return e;
+  if ((e = nle_stage(c, B, vk::ST_ETD_REF_3, S, C, S)) != cudaSuccess) return e;
+  if (!Snext) return cudaSuccess;
+  return nle_stage(c, C, vk::ST_ETD_4, S, C, Snext);
+}
+
+int adj_supported(vk_ctx* c) {
+  if (!c->has_state) return fail(c, VK_ERR_STATE, "no state set");
+  if (c->cfg.dt_mode != VK_DT_FIXED)
+    return fail(c, VK_ERR_UNSUPPORTED, "the adjoint needs dt_mode = fixed (the CFL dt is not differentiable)");
+  if (c->cfg.integrator != VK_INTEGRATOR_ETD_RK4 || c->cfg.etd_variant != VK_ETD_REFERENCE)
+    return fail(c, VK_ERR_UNSUPPORTED, "the adjoint is built for the reference ETD-RK4 variant");
+  return VK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vk_adjoint_forward(vk_ctx* c, int64_t nsteps, int32_t nsnap, double* J) {
+  if (!c || !J) return VK_ERR_INVALID;
+  int r = adj_supported(c);
+  if (r != VK_OK) return r;
+  if (nsteps < 1 || nsnap < 1) return fail(c, VK_ERR_INVALID, "nsteps >= 1 and nsnap >= 1 required");
+  DeviceGuard g(c->cfg.device);
+  const int64_t K = (nsteps + nsnap - 1) / nsnap;
+  const int64_t nseg = (nsteps + K - 1) / K;
+  cudaError_t e = adj_alloc(c, nseg, K);
+  if (e != cudaSuccess) {
+    free_adjoint(c);
+    return cuda_fail(c, e, "adjoint buffers");
+  }
+  auto& a = c->adj;
+  a.nsteps = nsteps;
+  a.ready = false;
+  const size_t sb = state_bytes(c);
+  for (int64_t s = 0; s < nseg; ++s) {
+    VK_CHECK(c, cudaMemcpyAsync(a.ckpt[(size_t)s], c->u, sb, cudaMemcpyDeviceToDevice, c->stream));
+    const int64_t ks = std::min<int64_t>(K, nsteps - s * K);
+    for (int64_t j = 0; j < ks; ++j) VK_CHECK(c, step_once(c));
+  }
+  // J = enstrophy of the final state and its raw-Euclidean cotangent
+  VK_CHECK(c, tier1_enqueue(c));
+  VK_CHECK(c, adj_mode(c, c->u, a.ub, 0));
+  vk::DevScalars h;
+  int rr = read_scalars(c, &h);
+  if (rr != VK_OK) return rr;
+  const double ntot = (double)c->N * (double)c->N * (double)c->N;
+  a.J = h.sums[1] / (ntot * ntot);
+  a.ready = true;
+  *J = a.J;
+  return VK_OK;
+}
+
+int vk_adjoint_backward(vk_ctx* c, double* gx, double* gy, double* gz) {
+  if (!c || !gx || !gy || !gz) return VK_ERR_INVALID;
+  if (!c->adj.ready) return fail(c, VK_ERR_STATE, "vk_adjoint_backward needs a preceding vk_adjoint_forward");
+  DeviceGuard g(c->cfg.device);
+  auto& a = c->adj;
+  const int64_t K = a.K;
+  void** S = a.seg.data();
+  void** A = S + (K + 1);
+  void** B = A + K;
+  void** C = B + K;
+  const size_t sb = state_bytes(c);
+  for (int64_t s = a.nseg - 1; s >= 0; --s) {
+    const int64_t ks = std::min<int64_t>(K, a.nsteps - s * K);
+    VK_CHECK(c, cudaMemcpyAsync(S[0], a.ckpt[(size_t)s], sb, cudaMemcpyDeviceToDevice, c->stream));
+    for (int64_t j = 0; j < ks; ++j)
+      VK_CHECK(c, forward_step_store(c, S[j], A[j], B[j], C[j], j + 1 < ks ? S[j + 1] : nullptr));
+    for (int64_t j = ks - 1; j >= 0; --j) VK_CHECK(c, adjoint_step(c, S[j], A[j], B[j], C[j]));
+  }
+  // gradient in the L2 inner product of the physical fields, projected on
+  // real, divergence-free, Nyquist-free fields
+  VK_CHECK(c, adj_mode(c, a.ub, a.acc, 1));
+  VK_CHECK(c, herm_avg(c, a.acc, a.nb));
+  a.ready = false;
+  return download_state(c, a.nb, gx, gy, gz);
+}
+
+int vk_nonlinear_adjoint_host(vk_ctx* c, const double* ux, const double* uy, const double* uz, const double* bx,
+                              const double* by, const double* bz, double* ox, double* oy, double* oz) {
+  if (!c) return VK_ERR_INVALID;
+  DeviceGuard g(c->cfg.device);
+  cudaError_t e = adj_alloc(c, std::max<int64_t>(c->adj.nseg, 1), std::max<int64_t>(c->adj.K, 1));
+  if (e != cudaSuccess) return cuda_fail(c, e, "adjoint buffers");
+  int r = upload_state(c, c->temp, ux, uy, uz);
+  if (r != VK_OK) return r;
+  r = upload_state(c, c->adj.nb, bx, by, bz);
+  if (r != VK_OK) return r;
+  VK_CHECK(c, nla(c, c->temp, c->adj.nb, -1, vk::ADJ_NL_OUT, c->n1));
+  return download_state(c, c->n1, ox, oy, oz);
+}
+
 int vk_step_timed(vk_ctx* c, int64_t nsteps, double* elapsed_ms) {
   if (!c || !elapsed_ms) return VK_ERR_INVALID;
   if (!c->has_state) return fail(c, VK_ERR_STATE, "vk_step_timed before vk_set_state_host");
@@ -765,7 +1010,8 @@ const char* vk_profile_pass_name(int32_t id) {
   static const char* names[vk::PASS_COUNT] = {
       "P1_x_inverse_pad_curl", "P2_y_inverse_pad_omega", "P3_z_c2r_cross_r2c", "P4_y_forward_trunc",
       "P5_x_forward_trunc_leray_stage", "NX_ngrid_x_inverse", "NY_ngrid_y_inverse", "NZ_ngrid_z_c2r_max",
-      "ETD_table", "small_scalar_kernels", "tier1_sums", "spectrum", "fft_z", "fft_y", "fft_x"};
+      "ETD_table", "small_scalar_kernels", "tier1_sums", "spectrum", "fft_z", "fft_y", "fft_x",
+      "A1_adj_x_inverse", "A2_adj_y_inverse", "A3_adj_z_cross", "A4_adj_y_forward", "A5_adj_x_forward_stage"};
   return id >= 0 && id < vk::PASS_COUNT ? names[id] : "";
 }
 

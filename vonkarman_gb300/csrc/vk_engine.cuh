@@ -3,6 +3,9 @@
 // vk_engine_f32.cu) so the two compile in parallel.
 #pragma once
 
+#include <algorithm>
+
+#include "vk_adjoint.cuh"
 #include "vk_reduce.cuh"
 
 namespace vk {
@@ -97,6 +100,68 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     const double scale = (double)M * M * M / ((double)N * N * N);
     P5Args<R> a{N, M, H, nzt5, (R)(1.0 / scale), ks, p.bufB, fsB4, p.st};
+    kern<<<nzt5 * N, NT, smem, s>>>(a, p.twM);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+template <typename R, int N>
+inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
+  constexpr int M = 3 * N / 2;
+  constexpr int H = N / 2 + 1;
+  constexpr int TZ = TZof<R>::value;
+  const int nzt = (H + TZ - 1) / TZ;
+  const size_t fsA1 = (size_t)M * N * H;   // A1 out: 8 fields (M, N, H)
+  const size_t fsB2 = (size_t)M * M * H;   // A2 out: 9 fields (M, M, H)
+  const size_t fsA3 = (size_t)M * M * H;   // A3 out: 6 fields (M, M, H)
+  const size_t fsB4 = (size_t)M * N * H;   // A4 out: 6 fields (M, N, H)
+  const R ks = (R)p.ks;
+  const double scale = (double)M * M * M / ((double)N * N * N);
+  cudaError_t e;
+  {
+    TimerScope ts(p.timer, PASS_A1, s);
+    OpAdjXInv<R> o{8, nzt, H, M, N, M, (R)(1.0 / ((double)N * N * N)), (R)(1.0 / scale), ks,
+                   p.x, p.cs, p.nb, p.etd, p.slot, p.fac, p.dt, p.bufA, fsA1};
+    e = launch_strided<R, M, true, TZ>(o, 8 * nzt * N, p.twM, s);
+    if (e != cudaSuccess) return e;
+  }
+  {
+    TimerScope ts(p.timer, PASS_A2, s);
+    OpAdjYInv<R> o{OpYInv<R>{6, nzt, H, M, N, M, 0, ks, p.bufA, fsA1, p.bufB, fsB2}, 9, nzt, H, M};
+    e = launch_strided<R, M, true, TZ>(o, 9 * nzt * M, p.twM, s);
+    if (e != cudaSuccess) return e;
+  }
+  {
+    TimerScope ts(p.timer, PASS_A3, s);
+    constexpr int CP = zpairs<M, 384>();
+    constexpr int NT = zthreads<9 * CP, M>();
+    const size_t smem = (size_t)9 * CP * M * sizeof(C2<R>);
+    constexpr auto kern = k_adj_z<R, M, CP, NT>;
+    e = prepare_kernel<kern>(smem);
+    if (e != cudaSuccess) return e;
+    A3Args<R> a{M * M, p.bufB, fsB2, p.bufA, fsA3};
+    const int nb = (M * M + 2 * CP - 1) / (2 * CP);
+    kern<<<nb, NT, smem, s>>>(a, p.twM);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  {
+    TimerScope ts(p.timer, PASS_A4, s);
+    OpYFwdTrunc<R> o{6, nzt, H, N, N, M, p.bufA, fsA3, p.bufB, fsB4};
+    e = launch_strided<R, M, false, TZ>(o, 6 * nzt * M, p.twM, s);
+    if (e != cudaSuccess) return e;
+  }
+  {
+    TimerScope ts(p.timer, PASS_A5, s);
+    constexpr int TZ5 = (sizeof(R) == 8 && M >= 768) ? 2 : TZ / 2;
+    constexpr int NT = cmax(64, cmin(1024, round32(TZ5 * M / 8)));
+    const int nzt5 = (H + TZ5 - 1) / TZ5;
+    const size_t smem = (size_t)(M + 5 * N) * TZ5 * sizeof(C2<R>);
+    constexpr auto kern = k_adj_p5<R, M, TZ5, NT>;
+    e = prepare_kernel<kern>(smem);
+    if (e != cudaSuccess) return e;
+    A5Args<R> a{N, M, H, nzt5, (R)(1.0 / ((double)N * N * N)), ks, p.bufB, fsB4, p.st};
     kern<<<nzt5 * N, NT, smem, s>>>(a, p.twM);
     e = cudaGetLastError();
   }
@@ -219,6 +284,34 @@ cudaError_t Engine<R>::nle(const NleParams<R>& p, cudaStream_t s) {
 #undef VK_CASE
     default: return cudaErrorInvalidValue;
   }
+}
+
+template <typename R>
+cudaError_t Engine<R>::nle_adjoint(const NlaParams<R>& p, cudaStream_t s) {
+  switch (p.N) {
+#define VK_CASE(NN) case NN: return nla_n<R, NN>(p, s);
+    VK_FOR_GRIDS(VK_CASE)
+#undef VK_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename R>
+cudaError_t Engine<R>::adj_mode(int N, double ks, size_t cs, const C2<R>* in, C2<R>* out, int mode,
+                                cudaStream_t s) {
+  ModeArgs<R> a{N, N / 2 + 1, ks, cs, in, out, mode};
+  const size_t total = (size_t)N * N * (N / 2 + 1);
+  const int nb = (int)std::min<size_t>((total + 255) / 256, 65536);
+  k_adj_mode<R><<<nb, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t Engine<R>::hermitian_avg(int N, size_t cs, const C2<R>* in, C2<R>* out, cudaStream_t s) {
+  const size_t total = (size_t)N * N * (N / 2 + 1);
+  const int nb = (int)std::min<size_t>((total + 255) / 256, 65536);
+  k_hermitian_avg<R><<<nb, 256, 0, s>>>(N, N / 2 + 1, cs, in, out);
+  return cudaGetLastError();
 }
 
 template <typename R>

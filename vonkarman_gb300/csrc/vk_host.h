@@ -57,6 +57,7 @@ template <typename R> struct StageArgs {
   int op;
   size_t cs;                       // component stride of spectral arrays
   C2<R>* u; C2<R>* temp; C2<R>* n1; C2<R>* acc; C2<R>* out;
+  C2<R>* u_out;                    // where the last ETD stage writes u_{n+1} (normally u)
   const double* etd;               // table, ETD_STRIDE doubles per |k|^2 index
   const double* dt;                // device scalar
   double nu;
@@ -68,6 +69,7 @@ enum Pass : int {
   PASS_P1 = 0, PASS_P2, PASS_P3, PASS_P4, PASS_P5,
   PASS_NX, PASS_NY, PASS_NZ, PASS_ETD, PASS_SMALL, PASS_TIER1, PASS_SPECTRUM,
   PASS_FFT_Z, PASS_FFT_Y, PASS_FFT_X,
+  PASS_A1, PASS_A2, PASS_A3, PASS_A4, PASS_A5,
   PASS_COUNT
 };
 struct KTimer {
@@ -110,6 +112,31 @@ template <typename R> struct FftParams {
   KTimer* timer;
 };
 
+// Adjoint stage combinations (see vk_adjoint.cuh).
+enum AdjOp : int { ADJ_NL_OUT = 0, ADJ_C = 1, ADJ_B = 2, ADJ_A = 3, ADJ_U = 4 };
+
+template <typename R> struct AdjStageArgs {
+  int op;
+  size_t cs;
+  C2<R>* ub; C2<R>* acc; C2<R>* nb; C2<R>* n1b; C2<R>* out;
+  const double* etd;
+  const double* dt;
+};
+
+// One adjoint nonlinear evaluation y = N'(x)^T nbar with a stage epilogue.
+template <typename R> struct NlaParams {
+  int N;
+  double ks;
+  const C2<R>* x; size_t cs;             // stage input
+  const C2<R>* nb;                       // cotangent source
+  const double* etd; int slot; double fac;   // nbar = fac dt etd[slot] nb if slot >= 0
+  const double* dt;
+  C2<R>* bufA; C2<R>* bufB;              // >= max(8 MNH, 6 M^2H), >= max(9 M^2H, 6 MNH)
+  const C2<R>* twM;
+  AdjStageArgs<R> st;
+  KTimer* timer;
+};
+
 template <typename R> struct Engine {
   static cudaError_t nle(const NleParams<R>& p, cudaStream_t s);
   static cudaError_t ngrid_max(const NgridParams<R>& p, cudaStream_t s);
@@ -119,6 +146,10 @@ template <typename R> struct Engine {
                                    cudaStream_t s);
   static cudaError_t spectrum_partial(const C2<R>* u, size_t cs, int N, double ks, int nsh, double* part,
                                       int nblk, cudaStream_t s);
+  static cudaError_t nle_adjoint(const NlaParams<R>& p, cudaStream_t s);
+  // mode 0: enstrophy cotangent of in; mode 1: weighted gradient (Nyquist-free, Leray)
+  static cudaError_t adj_mode(int N, double ks, size_t cs, const C2<R>* in, C2<R>* out, int mode, cudaStream_t s);
+  static cudaError_t hermitian_avg(int N, size_t cs, const C2<R>* in, C2<R>* out, cudaStream_t s);
 };
 extern template struct Engine<double>;
 extern template struct Engine<float>;

@@ -259,7 +259,7 @@ __device__ __forceinline__ void stage_apply(const StageArgs<R>& s, size_t idx, i
         const C2<R> a = s.acc[i];
         const R b4 = (R)e[E_B4];
         const C2<R> rhs = cmk<R>(a.x + b4 * n.x, a.y + b4 * n.y);
-        s.u[i] = axpby<R>((R)e[E_FULL], u, (R)dt, rhs);
+        s.u_out[i] = axpby<R>((R)e[E_FULL], u, (R)dt, rhs);
         break;
       }
       case ST_ETD_CM_1: {  // textbook: a = E2 u + (h/2) phi1(z/2) N1

@@ -222,7 +222,25 @@ def abc_plus_perturbation(n: int, rms: float = 1e-2, kp: float = 8.0, seed: int 
     return [a + b for a, b in zip(base, pert)]
 
 
+def project_control(u_hat, n: int, l: float = TWO_PI):
+    """Project onto real, divergence-free fields with zero Nyquist entries
+    (ix, iy or iz = n/2): with the convention kx[n/2] = -n/2 those entries
+    cannot be both Hermitian and divergence-free.  Orthogonal in the L2
+    inner product of the physical fields."""
+    out = []
+    for c in u_hat:
+        c = np.array(c, dtype=np.complex128, copy=True)
+        c[n // 2, :, :] = 0.0
+        c[:, n // 2, :] = 0.0
+        c[:, :, n // 2] = 0.0
+        out.append(c)
+    out = leray(out, n, l)
+    return [_r2c(_c2r(c, n)) for c in out]   # Hermitian part on the kz = 0 plane
+
+
 def solenoidal_direction(n: int, seed: int, kp: float = 4.0, l: float = TWO_PI):
-    """Seeded random divergence-free direction with unit L2 norm
-    (<|v|^2> = 1), for finite-difference gradient checks."""
-    return von_karman_isotropic(n, kp=kp, energy=0.5, seed=seed, l=l)
+    """Seeded random direction in the control space of the adjoint (real,
+    divergence-free, Nyquist-free) with unit L2 norm (<|v|^2> = 1)."""
+    v = project_control(von_karman_isotropic(n, kp=kp, energy=0.5, seed=seed, l=l), n, l)
+    e = spectral_energy(v, n)
+    return [c / np.sqrt(2.0 * e) for c in v]

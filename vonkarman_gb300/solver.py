@@ -219,6 +219,23 @@ class Periodic3D:
         return [ScalarDiagnostics._from_c(buf[i]) for i in range(got.value)]
 
 
+    # -- discrete adjoint (autograd-Function pattern) -------------------------
+    def adjoint_forward(self, nsteps: int, nsnap: int = 20) -> float:
+        """Run nsteps fixed-dt steps keeping nsnap checkpoints; returns
+        J = final enstrophy.  The state advances."""
+        v = ctypes.c_double()
+        self._call(self._lib.vk_adjoint_forward, int(nsteps), int(nsnap), ctypes.byref(v))
+        return v.value
+
+    def adjoint_backward(self):
+        """dJ/du_0 of the preceding adjoint_forward, in the L2 inner product of
+        the physical fields, projected on real divergence-free Nyquist-free
+        fields."""
+        shp = self.grid.spectral_shape
+        out = [np.empty(shp, dtype=np.complex128) for _ in range(3)]
+        self._call(self._lib.vk_adjoint_backward, *[nat.dptr(c) for c in out])
+        return out
+
     # -- measurement ----------------------------------------------------------
     def step_timed(self, nsteps: int) -> float:
         """Enqueue nsteps steps between two CUDA events on the context's
@@ -294,6 +311,27 @@ def compute_nonlinear(solver: Periodic3D, u_hat):
     nat.check(lib.vk_nonlinear_host(solver._ctx, *[nat.dptr(c) for c in ins], *[nat.dptr(c) for c in outs]),
               lib, solver._ctx)
     return outs
+
+
+def nonlinear_adjoint(solver: Periodic3D, x, nbar):
+    """N'(x)^T nbar in the raw Euclidean inner product of the stored entries."""
+    lib = solver._lib
+    shp = solver.grid.spectral_shape
+    xs = [_as_c128(c, shp) for c in x]
+    bs = [_as_c128(c, shp) for c in nbar]
+    outs = [np.empty(shp, dtype=np.complex128) for _ in range(3)]
+    nat.check(lib.vk_nonlinear_adjoint_host(solver._ctx, *[nat.dptr(c) for c in xs], *[nat.dptr(c) for c in bs],
+                                            *[nat.dptr(c) for c in outs]), lib, solver._ctx)
+    return outs
+
+
+def l2_inner(a, b, n: int) -> float:
+    """<a, b> = sum w Re(conj(a) b) / N^6, the L2 inner product of the physical
+    fields (R2C weights w = 1 at iz in {0, n/2}, else 2)."""
+    w = np.full(n // 2 + 1, 2.0)
+    w[0] = w[n // 2] = 1.0
+    nt2 = float(n) ** 6
+    return float(sum((w * (np.conj(x) * y).real).sum() for x, y in zip(a, b))) / nt2
 
 
 class GpuFftBackend:

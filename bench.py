@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=100,
+                    help="steps of the checkpointed adjoint measurement (0 = skip)")
     ap.add_argument("--precision", choices=["fp64", "fp32bulk"], default="fp64",
                     help="form of the headline run (fp32bulk only for profiling that form)")
     return ap.parse_args()
@@ -294,6 +296,51 @@ def timed_run(s, steps: int, spec_every: int):
     return s.event_elapsed(0, 1), specs
 
 
+def measure_adjoint(args, grid, dev, d: Dist):
+    """Checkpointed discrete adjoint on the checkpointed-ascent workload:
+    random isotropic start (kp=3, E=0.5), nu=2e-3, fixed dt=1e-3, 20 level-1
+    checkpoints, FP32-bulk; cost relative to a plain forward run of the same
+    steps, and the FP32-bulk gradient against the FP64 one on a shorter run."""
+    import vonkarman_gb300 as vk
+    from vonkarman_gb300 import ics
+
+    n, nu, dt = grid.n, 2e-3, 1e-3
+    u0 = ics.project_control(ics.von_karman_isotropic(n, kp=3.0, energy=0.5, seed=42), n)
+    k = args.adjoint_steps
+    opts = vk.SolverOptions(precision="fp32bulk", dt_mode="fixed", dt_fixed=dt, device=dev)
+    s = vk.Periodic3D(grid, nu, u0, opts)
+    s.step(2)
+    s.restore_state(u0, 0.0, 0, dt)
+    s.event_mark(0)
+    s.step(k)
+    s.event_mark(1)
+    fwd_ms = d.max(s.event_elapsed(0, 1))
+    s.restore_state(u0, 0.0, 0, dt)
+    s.event_mark(2)
+    s.adjoint_forward(k, 20)
+    s.event_mark(3)
+    g32 = s.adjoint_backward()
+    s.event_mark(4)
+    af_ms = d.max(s.event_elapsed(2, 3))
+    ab_ms = d.max(s.event_elapsed(3, 4))
+    s.close()
+    # FP32-bulk vs FP64 gradient on 20 steps
+    kk = min(20, k)
+    grads = []
+    for prec in ("fp64", "fp32bulk"):
+        t = vk.Periodic3D(grid, nu, u0, vk.SolverOptions(precision=prec, dt_mode="fixed", dt_fixed=dt, device=dev))
+        t.adjoint_forward(kk, 20)
+        grads.append(t.adjoint_backward())
+        t.close()
+    num = math.sqrt(sum(float(np.sum(np.abs(a - b) ** 2)) for a, b in zip(grads[1], grads[0])))
+    den = math.sqrt(sum(float(np.sum(np.abs(b) ** 2)) for b in grads[0]))
+    return {"workload": f"random isotropic kp=3 E=0.5, N={n}, nu=2e-3, fixed dt=1e-3, {k} steps, "
+                        "20 level-1 checkpoints, FP32-bulk",
+            "forward_ms": fwd_ms, "adjoint_forward_ms": af_ms, "adjoint_backward_ms": ab_ms,
+            "backward_over_forward": ab_ms / fwd_ms, "total_over_forward": (af_ms + ab_ms) / fwd_ms,
+            "fp32_vs_fp64_gradient_rel_l2": num / den, "gradient_check_steps": kk}
+
+
 def run_ours(args, d: Dist):
     import vonkarman_gb300 as vk
     from vonkarman_gb300 import ics
@@ -415,6 +462,10 @@ def run_ours(args, d: Dist):
             }
         s32.close()
 
+    adjoint = None
+    if args.adjoint_steps > 0 and args.precision == "fp64":
+        adjoint = measure_adjoint(args, grid, dev, d)
+
     cpu = None
     if d.rank == 0 and d.world == 1 and not args.no_cpu_baseline:
         cores = host_cores()
@@ -447,6 +498,7 @@ def run_ours(args, d: Dist):
         "gpu_launches": gpu_launches,
         "clocks": clocks,
         "fp32bulk": fp32,
+        "adjoint": adjoint,
         "sps_per_rank": sps_rank,
     }
     print(json.dumps(line), flush=True)

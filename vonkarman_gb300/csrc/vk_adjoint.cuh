@@ -103,34 +103,46 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_adj_z(A3Args<R> a, con
   constexpr int N = 2 * M / 3;
   constexpr int H = N / 2 + 1;
   constexpr int NL = 9 * CP;
+  constexpr int LP = zpad_len<R>(M);
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
   const int col0 = blockIdx.x * 2 * CP;
-  for (int e = threadIdx.x; e < 2 * CP * 4 * H; e += NT) {
+  constexpr int TOT = 2 * CP * 4 * H;
+  constexpr int PER = (TOT + NT - 1) / NT;
+  C2<R> lx[PER], ly[PER];
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * NT;
     const int k = e % H;
     const int t = (e / H) % 4;
-    const int cr = e / (4 * H);
-    const int col = col0 + cr;
-    C2<R> X = czero<R>(), Y = czero<R>();
-    if (col < a.ncols) {
-      X = a.in[(size_t)(2 * t) * a.fsin + (size_t)col * H + k];
-      Y = a.in[(size_t)(2 * t + 1) * a.fsin + (size_t)col * H + k];
+    const int col = col0 + e / (4 * H);
+    const bool ok = e < TOT && col < a.ncols;
+    lx[q] = ok ? a.in[(size_t)(2 * t) * a.fsin + (size_t)col * H + k] : czero<R>();
+    ly[q] = ok ? a.in[(size_t)(2 * t + 1) * a.fsin + (size_t)col * H + k] : czero<R>();
+  }
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * NT;
+    if (e < TOT) {
+      const int k = e % H;
+      const int t = (e / H) % 4;
+      const int cr = e / (4 * H);
+      zpack<R>(lines + (9 * (cr / 2) + 4 * (cr % 2) + t) * LP, M, k, lx[q], ly[q]);
     }
-    zpack<R>(lines + (9 * (cr / 2) + 4 * (cr % 2) + t) * M, M, k, X, Y);
   }
   for (int e = threadIdx.x; e < CP * H; e += NT) {
     const int k = e % H, pr = e / H;
     const int c0 = col0 + 2 * pr;
     const C2<R> X = c0 < a.ncols ? a.in[(size_t)8 * a.fsin + (size_t)c0 * H + k] : czero<R>();
     const C2<R> Y = c0 + 1 < a.ncols ? a.in[(size_t)8 * a.fsin + (size_t)(c0 + 1) * H + k] : czero<R>();
-    zpack<R>(lines + (9 * pr + 8) * M, M, k, X, Y);
+    zpack<R>(lines + (9 * pr + 8) * LP, M, k, X, Y);
   }
   for (int e = threadIdx.x; e < NL * (N / 2 - 1); e += NT) {
     const int l = e / (N / 2 - 1), p = H + e % (N / 2 - 1);
-    lines[l * M + p] = czero<R>();
+    lines[l * LP + zi<R>(p)] = czero<R>();
   }
   __syncthreads();
-  fft_smem<R, M, true, NT, NL, false>(lines, M, 1, tw);
+  fft_zlines<R, M, true, NT, NL>(lines, tw);
   constexpr int QX = (CP * M + NT - 1) / NT;
   C2<R> res[QX][6];
 #pragma unroll
@@ -138,11 +150,11 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_adj_z(A3Args<R> a, con
     const int e = threadIdx.x + q * NT;
     if (e < CP * M) {
       const int pr = e / M, p = e % M;
-      const C2<R> Z = lines[(9 * pr + 8) * M + p];
+      const C2<R> Z = lines[(9 * pr + 8) * LP + zi<R>(p)];
 #pragma unroll
       for (int cc = 0; cc < 2; ++cc) {
-        const C2<R>* L0 = lines + (9 * pr + 4 * cc) * M;
-        const C2<R> A = L0[p], B = L0[M + p], C = L0[2 * M + p], D = L0[3 * M + p];
+        const C2<R>* L0 = lines + (9 * pr + 4 * cc) * LP;
+        const C2<R> A = L0[zi<R>(p)], B = L0[LP + zi<R>(p)], C = L0[2 * LP + zi<R>(p)], D = L0[3 * LP + zi<R>(p)];
         const R ux = A.x, uy = A.y, uz = B.x, wx = B.y, wy = C.x, wz = C.y;
         const R cx = D.x, cy = D.y, cz = cc == 0 ? Z.x : Z.y;
         // a_bar = w x cb ; o_bar = cb x u
@@ -161,11 +173,11 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_adj_z(A3Args<R> a, con
     if (e < CP * M) {
       const int pr = e / M, p = e % M;
 #pragma unroll
-      for (int j = 0; j < 6; ++j) lines[(6 * pr + j) * M + p] = res[q][j];
+      for (int j = 0; j < 6; ++j) lines[(6 * pr + j) * LP + zi<R>(p)] = res[q][j];
     }
   }
   __syncthreads();
-  fft_smem<R, M, false, NT, 6 * CP, false>(lines, M, 1, tw);
+  fft_zlines<R, M, false, NT, 6 * CP>(lines, tw);
   for (int e = threadIdx.x; e < CP * 6 * H; e += NT) {
     const int k = e % H;
     const int j = (e / H) % 6;
@@ -174,7 +186,7 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_adj_z(A3Args<R> a, con
     const int col = col0 + 2 * pr + cc;
     if (col >= a.ncols) continue;
     C2<R> X, Y;
-    zunpack<R>(lines + (6 * pr + j) * M, M, k, X, Y);
+    zunpack<R>(lines + (6 * pr + j) * LP, M, k, X, Y);
     a.out[(size_t)(2 * t) * a.fsout + (size_t)col * H + k] = X;
     a.out[(size_t)(2 * t + 1) * a.fsout + (size_t)col * H + k] = Y;
   }
@@ -258,11 +270,20 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_adj_p5(A5Args<R> a, co
   const int iy = blockIdx.x / a.nztiles;
   const int z0 = zt * TZ;
   const int H = a.H;
+  constexpr int PER = (L * TZ + NT - 1) / NT;
   for (int c = 0; c < 6; ++c) {
-    for (int e = threadIdx.x; e < L * TZ; e += NT) {
+    C2<R> ld[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = threadIdx.x + q * NT;
       const int p = e / TZ, b = e % TZ;
       const int z = z0 + b;
-      buf[e] = z < H ? a.in[(size_t)c * a.fsin + ((size_t)p * N + iy) * H + z] : czero<R>();
+      ld[q] = (e < L * TZ && z < H) ? a.in[(size_t)c * a.fsin + ((size_t)p * N + iy) * H + z] : czero<R>();
+    }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = threadIdx.x + q * NT;
+      if (e < L * TZ) buf[e] = ld[q];
     }
     __syncthreads();
     fft_smem<R, L, false, NT, TZ, true>(buf, 1, TZ, tw);

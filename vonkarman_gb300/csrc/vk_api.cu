@@ -74,6 +74,7 @@ vk::ContourConsts contour_consts() {
     c.sth[j] = 1.0 * std::sin(theta);
     c.cos_sth[j] = std::cos(c.sth[j]);
     c.sin_sth[j] = std::sin(c.sth[j]);
+    c.exp_cth[j] = std::exp(c.cth[j]);
   }
   return c;
 }

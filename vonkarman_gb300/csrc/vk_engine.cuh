@@ -29,14 +29,22 @@ inline cudaError_t prepare_kernel(size_t smem) {
 }
 
 // ---------------------------------------------------------------------------
+// Threads per strided CTA: one radix-8 butterfly per thread and stage in FP64
+// (bound by the FP64 pipe), two in FP32 (smaller CTAs, several per SM, so
+// load and compute phases of different CTAs overlap).
+template <typename R, int L, int TZ>
+__host__ __device__ constexpr int strided_nt() {
+  return cmax(64, cmin(1024, round32(TZ * L / max_radix<R>(L))));
+}
+
 template <typename R, int L, bool INV, int TZ, class Op>
-inline cudaError_t launch_strided(const Op& op, int nblocks, const C2<R>* tw, cudaStream_t s) {
-  constexpr int NT = cmax(64, cmin(1024, round32(TZ * L / 8)));
+inline cudaError_t launch_strided(const Op& op, int ntiles, const C2<R>* tw, cudaStream_t s) {
+  constexpr int NT = strided_nt<R, L, TZ>();
   const size_t smem = (size_t)L * TZ * sizeof(C2<R>);
   constexpr auto kern = k_strided<R, L, INV, TZ, NT, Op>;
   cudaError_t e = prepare_kernel<kern>(smem);
   if (e != cudaSuccess) return e;
-  kern<<<nblocks, NT, smem, s>>>(op, tw);
+  kern<<<ntiles, NT, smem, s>>>(op, tw);
   return cudaGetLastError();
 }
 
@@ -70,8 +78,8 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   {
     TimerScope ts(p.timer, PASS_P3, s);
     constexpr int CP = zpairs<M, 384>();
-    constexpr int NT = zthreads<6 * CP, M>();
-    const size_t smem = (size_t)6 * CP * M * sizeof(C2<R>);
+    constexpr int NT = zthreads<R, 6 * CP, M>();
+    const size_t smem = (size_t)6 * CP * zpad_len<R>(M) * sizeof(C2<R>);
     constexpr auto kern = k_p3<R, M, CP, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
@@ -92,7 +100,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   {
     TimerScope ts(p.timer, PASS_P5, s);
     constexpr int TZ5 = TZ / 2;
-    constexpr int NT = cmax(64, cmin(1024, round32(TZ5 * M / 8)));
+    constexpr int NT = cmax(64, cmin(1024, round32(TZ5 * M / max_radix<R>(M))));
     const int nzt5 = (H + TZ5 - 1) / TZ5;
     const size_t smem = (size_t)(M + 2 * N) * TZ5 * sizeof(C2<R>);
     constexpr auto kern = k_p5<R, M, TZ5, NT>;
@@ -135,8 +143,8 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
   {
     TimerScope ts(p.timer, PASS_A3, s);
     constexpr int CP = zpairs<M, 384>();
-    constexpr int NT = zthreads<9 * CP, M>();
-    const size_t smem = (size_t)9 * CP * M * sizeof(C2<R>);
+    constexpr int NT = zthreads<R, 9 * CP, M>();
+    const size_t smem = (size_t)9 * CP * zpad_len<R>(M) * sizeof(C2<R>);
     constexpr auto kern = k_adj_z<R, M, CP, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
@@ -155,7 +163,7 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
   {
     TimerScope ts(p.timer, PASS_A5, s);
     constexpr int TZ5 = (sizeof(R) == 8 && M >= 768) ? 2 : TZ / 2;
-    constexpr int NT = cmax(64, cmin(1024, round32(TZ5 * M / 8)));
+    constexpr int NT = cmax(64, cmin(1024, round32(TZ5 * M / max_radix<R>(M))));
     const int nzt5 = (H + TZ5 - 1) / TZ5;
     const size_t smem = (size_t)(M + 5 * N) * TZ5 * sizeof(C2<R>);
     constexpr auto kern = k_adj_p5<R, M, TZ5, NT>;
@@ -198,15 +206,15 @@ inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
   NZArgs<R> a{N * N, p.bufB, fs, p.out, p.which};
   const int nb = (N * N + 2 * CP - 1) / (2 * CP);
   if (both) {
-    constexpr int NT = zthreads<6 * CP, N>();
-    const size_t smem = (size_t)6 * CP * N * sizeof(C2<R>);
+    constexpr int NT = zthreads<R, 6 * CP, N>();
+    const size_t smem = (size_t)6 * CP * zpad_len<R>(N) * sizeof(C2<R>);
     constexpr auto kern = k_nz_max<R, N, CP, true, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
     kern<<<nb, NT, smem, s>>>(a, p.twN);
   } else {
-    constexpr int NT = zthreads<3 * CP, N>();
-    const size_t smem = (size_t)3 * CP * N * sizeof(C2<R>);
+    constexpr int NT = zthreads<R, 3 * CP, N>();
+    const size_t smem = (size_t)3 * CP * zpad_len<R>(N) * sizeof(C2<R>);
     constexpr auto kern = k_nz_max<R, N, CP, false, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
@@ -219,8 +227,8 @@ inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
 template <typename R, int L>
 inline cudaError_t fz_pass(const FftParams<R>& p, bool inverse, R scale, cudaStream_t s) {
   constexpr int CP = zpairs<L, 4096>();
-  constexpr int NT = zthreads<CP, L>();
-  const size_t smem = (size_t)CP * L * sizeof(C2<R>);
+  constexpr int NT = zthreads<R, CP, L>();
+  const size_t smem = (size_t)CP * zpad_len<R>(L) * sizeof(C2<R>);
   const int ncols = p.nx * p.ny;
   const int nb = (ncols + 2 * CP - 1) / (2 * CP);
   FZArgs<R> a{ncols, p.real, p.cplx, scale};

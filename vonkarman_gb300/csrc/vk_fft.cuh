@@ -75,6 +75,46 @@ __host__ __device__ constexpr int plan_radix(int L, int s) {
        : 1;
 }
 
+// FP32 plans use in-register radix-16 stages: fewer shared-memory passes for
+// the bandwidth-bound FP32 form.  FP64 keeps radix <= 8 (registers; the FP64
+// form is bound by the FP64 pipe, where radix 16 saves no instructions).
+__host__ __device__ constexpr int plan_stages_f(int L) {
+  return L == 8 ? 1 : L == 16 ? 1 : L == 32 ? 2 : L == 64 ? 2 : L == 128 ? 2 : L == 256 ? 2
+       : L == 512 ? 3 : L == 1024 ? 3 : L == 12 ? 2 : L == 24 ? 2 : L == 48 ? 2 : L == 96 ? 3
+       : L == 192 ? 3 : L == 384 ? 3 : L == 768 ? 3 : L == 1536 ? 4 : -1;
+}
+
+__host__ __device__ constexpr int plan_radix_f(int L, int s) {
+  return L == 8 ? 8
+       : L == 16 ? 16
+       : L == 32 ? (s == 0 ? 16 : 2)
+       : L == 64 ? (s == 0 ? 16 : 4)
+       : L == 128 ? (s == 0 ? 16 : 8)
+       : L == 256 ? 16
+       : L == 512 ? (s < 2 ? 8 : 8)
+       : L == 1024 ? (s < 2 ? 16 : 4)
+       : L == 12 ? (s == 0 ? 4 : 3)
+       : L == 24 ? (s == 0 ? 8 : 3)
+       : L == 48 ? (s == 0 ? 16 : 3)
+       : L == 96 ? (s == 0 ? 16 : s == 1 ? 2 : 3)
+       : L == 192 ? (s == 0 ? 16 : s == 1 ? 4 : 3)
+       : L == 384 ? (s == 0 ? 16 : s == 1 ? 8 : 3)
+       : L == 768 ? (s < 2 ? 16 : 3)
+       : L == 1536 ? (s < 2 ? 16 : s == 2 ? 2 : 3)
+       : 1;
+}
+
+template <typename R> __host__ __device__ constexpr int stages_of(int L) {
+  return sizeof(R) == 4 ? plan_stages_f(L) : plan_stages(L);
+}
+template <typename R> __host__ __device__ constexpr int radix_of(int L, int s) {
+  return sizeof(R) == 4 ? plan_radix_f(L, s) : plan_radix(L, s);
+}
+// widest butterfly of a plan (threads per line = L / widest)
+template <typename R> __host__ __device__ constexpr int max_radix(int L) {
+  return sizeof(R) == 4 ? ((L % 16 == 0 && L >= 16 && L != 512) ? 16 : 8) : 8;
+}
+
 __host__ __device__ constexpr bool fft_len_supported(int L) { return plan_stages(L) > 0; }
 
 // ---------------------------------------------------------------------------
@@ -213,9 +253,42 @@ __device__ __forceinline__ void rad8(C2<R>* v, const C2<R>* w) {
   v[7] = cmk<R>(fma(-h, s3, e3.x), fma(-h, d3, e3.y));
 }
 
+// radix-16 = 4 x 4: 4-point DFTs over n1 of x[n1 + 4 n2] (stage twiddles fused),
+// internal twiddles W16^(n1 k2) fused into the second layer, output
+// X[4 k1 + k2] from the k2-th second-layer DFT.
+template <typename R, bool INV, bool TW>
+__device__ __forceinline__ void rad16(C2<R>* v, const C2<R>* w) {
+  const R c1 = R(0.92387953251128675612818318939678829);   // cos(pi/8)
+  const R s1 = R(0.38268343236508977172845998403039887);   // sin(pi/8)
+  const R h = R(0.70710678118654752440084436210484904);
+  const C2<R> one = cmk<R>(R(1), R(0));
+  C2<R> y[4][4];
+#pragma unroll
+  for (int n1 = 0; n1 < 4; ++n1) {
+    C2<R> a0 = v[n1];
+    if (TW && n1 > 0) a0 = tw_mul<R, INV>(w[n1], a0);
+    rad4_core<R, INV, TW>(a0, v[n1 + 4], v[n1 + 8], v[n1 + 12], TW ? w[n1 + 4] : one, TW ? w[n1 + 8] : one,
+                          TW ? w[n1 + 12] : one, y[n1][0], y[n1][1], y[n1][2], y[n1][3]);
+  }
+  // forward W16^m (m = n1 k2): conjugated for the inverse by tw_fma/tw_mul<INV>
+  const C2<R> W1 = cmk<R>(c1, -s1), W2 = cmk<R>(h, -h), W3 = cmk<R>(s1, -c1), W4 = cmk<R>(R(0), R(-1));
+  const C2<R> W6 = cmk<R>(-h, -h), W9 = cmk<R>(-c1, s1);
+  C2<R> x[4];
+  rad4_core<R, INV, false>(y[0][0], y[1][0], y[2][0], y[3][0], one, one, one, x[0], x[1], x[2], x[3]);
+  v[0] = x[0]; v[4] = x[1]; v[8] = x[2]; v[12] = x[3];
+  rad4_core<R, INV, true>(y[0][1], y[1][1], y[2][1], y[3][1], W1, W2, W3, x[0], x[1], x[2], x[3]);
+  v[1] = x[0]; v[5] = x[1]; v[9] = x[2]; v[13] = x[3];
+  rad4_core<R, INV, true>(y[0][2], y[1][2], y[2][2], y[3][2], W2, W4, W6, x[0], x[1], x[2], x[3]);
+  v[2] = x[0]; v[6] = x[1]; v[10] = x[2]; v[14] = x[3];
+  rad4_core<R, INV, true>(y[0][3], y[1][3], y[2][3], y[3][3], W3, W6, W9, x[0], x[1], x[2], x[3]);
+  v[3] = x[0]; v[7] = x[1]; v[11] = x[2]; v[15] = x[3];
+}
+
 template <typename R, bool INV, int RAD, bool TW>
 __device__ __forceinline__ void dft(C2<R>* v, const C2<R>* w) {
-  if constexpr (RAD == 8) {
+  if constexpr (RAD == 16) {
+    rad16<R, INV, TW>(v, w);
+  } else if constexpr (RAD == 8) {
     rad8<R, INV, TW>(v, w);
   } else if constexpr (RAD == 4) {
     rad4<R, INV, TW>(v, w);
@@ -227,15 +300,24 @@ __device__ __forceinline__ void dft(C2<R>* v, const C2<R>* w) {
 }
 
 // ---------------------------------------------------------------------------
-// Stockham stages.  Element p of line l lives at buf[l*ld_line + p*ld_elem].
+// Stockham stages.  Element p of line l lives at buf[l*ld_line + p*ld_elem],
+// or, for contiguous lines (ZPAD), at buf[l*ld_line + zi(p)] with one padding
+// element after every 8: the first stage writes at stride RAD, which would
+// otherwise put most lanes of a warp on the same shared-memory banks.
 // LINE_FAST: consecutive threads take consecutive lines (use when lines are
 // interleaved, ld_line == 1); otherwise consecutive butterflies of a line.
 // ---------------------------------------------------------------------------
-template <typename R, int L, bool INV, int NT, int NLINES, bool LINE_FAST, int S, int NS>
+// one padding element per 128-byte row of the line: 8 complex doubles or 16
+// complex floats
+template <typename R> __host__ __device__ constexpr int zrow() { return 128 / (2 * (int)sizeof(R)); }
+template <typename R> __host__ __device__ constexpr int zi(int p) { return p + p / zrow<R>(); }
+template <typename R> __host__ __device__ constexpr int zpad_len(int L) { return L + L / zrow<R>(); }
+
+template <typename R, int L, bool INV, int NT, int NLINES, bool LINE_FAST, int S, int NS, bool ZPAD = false>
 struct StockhamStage {
   __device__ __forceinline__ static void run(C2<R>* buf, int ld_line, int ld_elem,
                                              const C2<R>* __restrict__ tw) {
-    constexpr int RAD = plan_radix(L, S);
+    constexpr int RAD = radix_of<R>(L, S);
     constexpr int NB = L / RAD;          // butterflies per line
     constexpr int TOTAL = NB * NLINES;   // butterflies per stage
     constexpr int Q = (TOTAL + NT - 1) / NT;
@@ -250,7 +332,7 @@ struct StockhamStage {
         const int j = LINE_FAST ? (g / NLINES) : (g % NB);
         const C2<R>* src = buf + l * ld_line;
 #pragma unroll
-        for (int r = 0; r < RAD; ++r) v[q][r] = src[(j + r * NB) * ld_elem];
+        for (int r = 0; r < RAD; ++r) v[q][r] = src[ZPAD ? zi<R>(j + r * NB) : (j + r * NB) * ld_elem];
       }
     }
     __syncthreads();
@@ -270,23 +352,29 @@ struct StockhamStage {
         C2<R>* dst = buf + l * ld_line;
         const int base = (j - k) * RAD + k;
 #pragma unroll
-        for (int r = 0; r < RAD; ++r) dst[(base + r * NS) * ld_elem] = v[q][r];
+        for (int r = 0; r < RAD; ++r) dst[ZPAD ? zi<R>(base + r * NS) : (base + r * NS) * ld_elem] = v[q][r];
       }
     }
     __syncthreads();
-    if constexpr (S + 1 < plan_stages(L)) {
-      StockhamStage<R, L, INV, NT, NLINES, LINE_FAST, S + 1, NS * RAD>::run(buf, ld_line, ld_elem, tw);
+    if constexpr (S + 1 < stages_of<R>(L)) {
+      StockhamStage<R, L, INV, NT, NLINES, LINE_FAST, S + 1, NS * RAD, ZPAD>::run(buf, ld_line, ld_elem, tw);
     }
   }
 };
 
 // Transform NLINES lines held in shared memory.  Must be called by all NT
 // threads of the CTA; begins and ends with the data synchronised.
-template <typename R, int L, bool INV, int NT, int NLINES, bool LINE_FAST>
+template <typename R, int L, bool INV, int NT, int NLINES, bool LINE_FAST, bool ZPAD = false>
 __device__ __forceinline__ void fft_smem(C2<R>* buf, int ld_line, int ld_elem,
                                          const C2<R>* __restrict__ tw) {
-  static_assert(plan_stages(L) > 0, "unsupported FFT length");
-  StockhamStage<R, L, INV, NT, NLINES, LINE_FAST, 0, 1>::run(buf, ld_line, ld_elem, tw);
+  static_assert(stages_of<R>(L) > 0, "unsupported FFT length");
+  StockhamStage<R, L, INV, NT, NLINES, LINE_FAST, 0, 1, ZPAD>::run(buf, ld_line, ld_elem, tw);
+}
+
+// Contiguous padded lines of length L (line stride zpad_len(L)).
+template <typename R, int L, bool INV, int NT, int NLINES>
+__device__ __forceinline__ void fft_zlines(C2<R>* buf, const C2<R>* __restrict__ tw) {
+  fft_smem<R, L, INV, NT, NLINES, false, true>(buf, zpad_len<R>(L), 1, tw);
 }
 
 }  // namespace vk

@@ -41,6 +41,7 @@ struct ContourConsts {
   double sth[32];
   double cos_sth[32];
   double sin_sth[32];
+  double exp_cth[32];   // exp(cos theta_j)
 };
 
 // Stage epilogue selector (fused into the last pass of a nonlinear evaluation).

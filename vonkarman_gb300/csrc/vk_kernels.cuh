@@ -43,38 +43,48 @@ __host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 __host__ __device__ constexpr int round32(int a) { return (a + 31) / 32 * 32; }
 
-// Lines per CTA for the strided (x / y) passes: TZ consecutive iz values, so
-// each row segment is 128 bytes.
-template <typename R> struct TZof { static constexpr int value = sizeof(R) == 8 ? 8 : 16; };
-template <typename R, int L>
-__host__ __device__ constexpr int strided_threads() {
-  return cmax(64, cmin(1024, round32(TZof<R>::value * L / 8)));
-}
+// Lines per CTA for the strided (x / y) passes: TZ = 8 consecutive iz values
+// (128-byte row segments in FP64, 64 in FP32; small FP32 tiles let several
+// CTAs per SM overlap their load and compute phases).
+template <typename R> struct TZof { static constexpr int value = 8; };
 // z passes: column pairs per CTA so that CP * L == 768 (z-cross) / 512 (N grid)
 template <int L, int TARGET> __host__ __device__ constexpr int zpairs() { return cmax(1, TARGET / L); }
-template <int NLINES, int L>
-__host__ __device__ constexpr int zthreads() { return cmax(64, cmin(1024, round32(NLINES * L / 8))); }
+template <typename R, int NLINES, int L>
+__host__ __device__ constexpr int zthreads() { return cmax(64, cmin(1024, round32(NLINES * L / max_radix<R>(L)))); }
 // Minimum resident CTAs per SM requested from the compiler: enough for 24
 // warps per SM, which caps registers near 85 per thread.
 template <int NT> __host__ __device__ constexpr int min_blocks() { return cmax(1, 768 / NT); }
 
 // ---------------------------------------------------------------------------
 // Generic strided pass: one field of TZ interleaved lines per CTA.
-// blockIdx.x = f + nfields * (ztile + nztiles * outer)
+// blockIdx.x = f + nfields * (ztile + nztiles * outer).  All loads of a CTA
+// are issued into registers before the first shared-memory store, so each
+// thread has PER loads in flight.
 // ---------------------------------------------------------------------------
 template <typename R, int L, bool INV, int TZ, int NT, class Op>
 __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_strided(Op op, const C2<R>* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* buf = reinterpret_cast<C2<R>*>(vk_smem);
+  constexpr int PER = (L * TZ + NT - 1) / NT;
   const int f = blockIdx.x % op.nfields;
   const int rest = blockIdx.x / op.nfields;
-  const int zt = rest % op.nztiles;
+  const int z0 = (rest % op.nztiles) * TZ;
   const int outer = rest / op.nztiles;
-  const int z0 = zt * TZ;
-  for (int e = threadIdx.x; e < L * TZ; e += NT) {
-    const int p = e / TZ, b = e % TZ;
-    const int z = z0 + b;
-    buf[e] = (z < op.hz) ? op.load(f, outer, z, p) : czero<R>();
+  C2<R> ld[PER];
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * NT;
+    ld[q] = czero<R>();
+    if (e < L * TZ) {
+      const int p = e / TZ, b = e % TZ;
+      const int z = z0 + b;
+      if (z < op.hz) ld[q] = op.load(f, outer, z, p);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * NT;
+    if (e < L * TZ) buf[e] = ld[q];
   }
   __syncthreads();
   fft_smem<R, L, INV, NT, TZ, true>(buf, 1, TZ, tw);
@@ -314,11 +324,20 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_p5(P5Args<R> a, const 
   const int iy = blockIdx.x / a.nztiles;
   const int z0 = zt * TZ;
   const int H = a.H;
+  constexpr int PER = (L * TZ + NT - 1) / NT;
   for (int c = 0; c < 3; ++c) {
-    for (int e = threadIdx.x; e < L * TZ; e += NT) {
+    C2<R> ld[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = threadIdx.x + q * NT;
       const int p = e / TZ, b = e % TZ;
       const int z = z0 + b;
-      buf[e] = z < H ? a.in[(size_t)c * a.fsin + ((size_t)p * N + iy) * H + z] : czero<R>();
+      ld[q] = (e < L * TZ && z < H) ? a.in[(size_t)c * a.fsin + ((size_t)p * N + iy) * H + z] : czero<R>();
+    }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = threadIdx.x + q * NT;
+      if (e < L * TZ) buf[e] = ld[q];
     }
     __syncthreads();
     fft_smem<R, L, false, NT, TZ, true>(buf, 1, TZ, tw);
@@ -363,20 +382,21 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_p5(P5Args<R> a, const 
 // Unpacking after a forward FFT:  X[k] = (Z[k] + conj Z[-k]) / 2,
 //                                 Y[k] = (Z[k] - conj Z[-k]) / (2i).
 // ---------------------------------------------------------------------------
+// Lines are in the padded shared layout (position p at zi<R>(p)).
 template <typename R>
 __device__ __forceinline__ void zpack(C2<R>* line, int L, int k, C2<R> X, C2<R> Y) {
   if (k == 0 || 2 * k == L) {
-    line[k] = cmk<R>(X.x, Y.x);
+    line[zi<R>(k)] = cmk<R>(X.x, Y.x);
   } else {
-    line[k] = cmk<R>(X.x - Y.y, X.y + Y.x);
-    line[L - k] = cmk<R>(X.x + Y.y, Y.x - X.y);
+    line[zi<R>(k)] = cmk<R>(X.x - Y.y, X.y + Y.x);
+    line[zi<R>(L - k)] = cmk<R>(X.x + Y.y, Y.x - X.y);
   }
 }
 
 template <typename R>
 __device__ __forceinline__ void zunpack(const C2<R>* line, int L, int k, C2<R>& X, C2<R>& Y) {
-  const C2<R> z = line[k];
-  const C2<R> w = line[k == 0 ? 0 : L - k];
+  const C2<R> z = line[zi<R>(k)];
+  const C2<R> w = line[zi<R>(k == 0 ? 0 : L - k)];
   X = cmk<R>(R(0.5) * (z.x + w.x), R(0.5) * (z.y - w.y));
   Y = cmk<R>(R(0.5) * (z.y + w.y), R(0.5) * (w.x - z.x));
 }
@@ -399,29 +419,40 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_p3(P3Args<R> a, const 
   constexpr int N = 2 * M / 3;
   constexpr int H = N / 2 + 1;
   constexpr int NL = 6 * CP;
+  constexpr int LP = zpad_len<R>(M);
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
   const int col0 = blockIdx.x * 2 * CP;
-  // load + pack
-  for (int e = threadIdx.x; e < 2 * CP * 3 * H; e += NT) {
+  // load + pack (all loads of a thread issued before the packing stores)
+  constexpr int TOT = 2 * CP * 3 * H;
+  constexpr int PER = (TOT + NT - 1) / NT;
+  C2<R> lx[PER], ly[PER];
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * NT;
     const int k = e % H;
     const int t = (e / H) % 3;
-    const int cr = e / (3 * H);
-    const int col = col0 + cr;
-    C2<R> X = czero<R>(), Y = czero<R>();
-    if (col < a.ncols) {
-      X = a.in[(size_t)(2 * t) * a.fsin + (size_t)col * H + k];
-      Y = a.in[(size_t)(2 * t + 1) * a.fsin + (size_t)col * H + k];
+    const int col = col0 + e / (3 * H);
+    const bool ok = e < TOT && col < a.ncols;
+    lx[q] = ok ? a.in[(size_t)(2 * t) * a.fsin + (size_t)col * H + k] : czero<R>();
+    ly[q] = ok ? a.in[(size_t)(2 * t + 1) * a.fsin + (size_t)col * H + k] : czero<R>();
+  }
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * NT;
+    if (e < TOT) {
+      const int k = e % H;
+      const int t = (e / H) % 3;
+      const int cr = e / (3 * H);
+      zpack<R>(lines + (6 * (cr / 2) + 3 * (cr % 2) + t) * LP, M, k, lx[q], ly[q]);
     }
-    C2<R>* line = lines + (6 * (cr / 2) + 3 * (cr % 2) + t) * M;
-    zpack<R>(line, M, k, X, Y);
   }
   for (int e = threadIdx.x; e < NL * (N / 2 - 1); e += NT) {
     const int l = e / (N / 2 - 1), p = H + e % (N / 2 - 1);
-    lines[l * M + p] = czero<R>();
+    lines[l * LP + zi<R>(p)] = czero<R>();
   }
   __syncthreads();
-  fft_smem<R, M, true, NT, NL, false>(lines, M, 1, tw);
+  fft_zlines<R, M, true, NT, NL>(lines, tw);
   // cross product, two phases (all reads, sync, all writes)
   constexpr int QX = (CP * M + NT - 1) / NT;
   C2<R> res[QX][3];
@@ -433,8 +464,8 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_p3(P3Args<R> a, const 
       R cz[2];
 #pragma unroll
       for (int cc = 0; cc < 2; ++cc) {
-        const C2<R>* L0 = lines + (6 * pr + 3 * cc) * M;
-        const C2<R> A = L0[p], B = L0[M + p], C = L0[2 * M + p];
+        const C2<R>* L0 = lines + (6 * pr + 3 * cc) * LP;
+        const C2<R> A = L0[zi<R>(p)], B = L0[LP + zi<R>(p)], C = L0[2 * LP + zi<R>(p)];
         const R ux = A.x, uy = A.y, uz = B.x, wx = B.y, wy = C.x, wz = C.y;
         res[q][cc] = cmk<R>(uy * wz - uz * wy, uz * wx - ux * wz);
         cz[cc] = ux * wy - uy * wx;
@@ -449,18 +480,18 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_p3(P3Args<R> a, const 
     if (e < CP * M) {
       const int pr = e / M, p = e % M;
 #pragma unroll
-      for (int j = 0; j < 3; ++j) lines[(3 * pr + j) * M + p] = res[q][j];
+      for (int j = 0; j < 3; ++j) lines[(3 * pr + j) * LP + zi<R>(p)] = res[q][j];
     }
   }
   __syncthreads();
-  fft_smem<R, M, false, NT, 3 * CP, false>(lines, M, 1, tw);
+  fft_zlines<R, M, false, NT, 3 * CP>(lines, tw);
   // unpack + store H modes of c_x, c_y, c_z for both columns of each pair
   for (int e = threadIdx.x; e < CP * 3 * H; e += NT) {
     const int k = e % H;
     const int j = (e / H) % 3;
     const int pr = e / (3 * H);
     C2<R> X, Y;
-    zunpack<R>(lines + (3 * pr + j) * M, M, k, X, Y);
+    zunpack<R>(lines + (3 * pr + j) * LP, M, k, X, Y);
     const int c0 = col0 + 2 * pr;
     if (j < 2) {
       const int col = c0 + j;
@@ -499,6 +530,7 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_nz_max(NZArgs<R> a, co
   constexpr int H = N / 2 + 1;
   constexpr int LPP = BOTH ? 6 : 3;   // lines per column pair
   constexpr int NL = LPP * CP;
+  constexpr int LP = zpad_len<R>(N);
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
   __shared__ double red[2][32];
@@ -517,7 +549,7 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_nz_max(NZArgs<R> a, co
         X = a.in[(size_t)(2 * t) * a.fs + (size_t)col * H + k];
         Y = a.in[(size_t)(2 * t + 1) * a.fs + (size_t)col * H + k];
       }
-      zpack<R>(lines + (6 * pr + 3 * cc + t) * N, N, k, X, Y);
+      zpack<R>(lines + (6 * pr + 3 * cc + t) * LP, N, k, X, Y);
     } else {
       // t in {0}: each column loads its f0/f1 pair; the f2 fields of the two
       // columns of a pair share one line.
@@ -525,7 +557,7 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_nz_max(NZArgs<R> a, co
         X = a.in[(size_t)col * H + k];
         Y = a.in[a.fs + (size_t)col * H + k];
       }
-      zpack<R>(lines + (3 * pr + cc) * N, N, k, X, Y);
+      zpack<R>(lines + (3 * pr + cc) * LP, N, k, X, Y);
     }
   }
   if (!BOTH) {
@@ -535,11 +567,11 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_nz_max(NZArgs<R> a, co
       C2<R> X = czero<R>(), Y = czero<R>();
       if (c0 < a.ncols) X = a.in[2 * a.fs + (size_t)c0 * H + k];
       if (c0 + 1 < a.ncols) Y = a.in[2 * a.fs + (size_t)(c0 + 1) * H + k];
-      zpack<R>(lines + (3 * pr + 2) * N, N, k, X, Y);
+      zpack<R>(lines + (3 * pr + 2) * LP, N, k, X, Y);
     }
   }
   __syncthreads();
-  fft_smem<R, N, true, NT, NL, false>(lines, N, 1, tw);
+  fft_zlines<R, N, true, NT, NL>(lines, tw);
   double m1 = 0.0, m2 = 0.0;
   int bad = 0;
   for (int e = threadIdx.x; e < CP * N; e += NT) {
@@ -548,8 +580,8 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_nz_max(NZArgs<R> a, co
     for (int cc = 0; cc < 2; ++cc) {
       if (col0 + 2 * pr + cc >= a.ncols) continue;
       if (BOTH) {
-        const C2<R>* L0 = lines + (6 * pr + 3 * cc) * N;
-        const C2<R> A = L0[p], B = L0[N + p], C = L0[2 * N + p];
+        const C2<R>* L0 = lines + (6 * pr + 3 * cc) * LP;
+        const C2<R> A = L0[zi<R>(p)], B = L0[LP + zi<R>(p)], C = L0[2 * LP + zi<R>(p)];
         const double ux = A.x, uy = A.y, uz = B.x, wx = B.y, wy = C.x, wz = C.y;
         const double s1 = ux * ux + uy * uy + uz * uz;
         const double s2 = wx * wx + wy * wy + wz * wz;
@@ -557,8 +589,8 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_nz_max(NZArgs<R> a, co
         m1 = fmax(m1, s1);
         m2 = fmax(m2, s2);
       } else {
-        const C2<R> A = lines[(3 * pr + cc) * N + p];
-        const C2<R> Z = lines[(3 * pr + 2) * N + p];
+        const C2<R> A = lines[(3 * pr + cc) * LP + zi<R>(p)];
+        const C2<R> Z = lines[(3 * pr + 2) * LP + zi<R>(p)];
         const double fx = A.x, fy = A.y, fz = cc == 0 ? Z.x : Z.y;
         const double s = fx * fx + fy * fy + fz * fz;
         bad |= (s != s);
@@ -603,6 +635,7 @@ template <typename R> struct FZArgs {
 template <typename R, int L, int CP, int NT>
 __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_fz_r2c(FZArgs<R> a, const C2<R>* __restrict__ tw) {
   constexpr int H = L / 2 + 1;
+  constexpr int LP = zpad_len<R>(L);
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
   const int col0 = blockIdx.x * 2 * CP;
@@ -611,15 +644,15 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_fz_r2c(FZArgs<R> a, co
     const int c0 = col0 + 2 * pr;
     const R x = c0 < a.ncols ? a.real[(size_t)c0 * L + p] : R(0);
     const R y = c0 + 1 < a.ncols ? a.real[(size_t)(c0 + 1) * L + p] : R(0);
-    lines[pr * L + p] = cmk<R>(x, y);
+    lines[pr * LP + zi<R>(p)] = cmk<R>(x, y);
   }
   __syncthreads();
-  fft_smem<R, L, false, NT, CP, false>(lines, L, 1, tw);
+  fft_zlines<R, L, false, NT, CP>(lines, tw);
   for (int e = threadIdx.x; e < CP * H; e += NT) {
     const int pr = e / H, k = e % H;
     const int c0 = col0 + 2 * pr;
     C2<R> X, Y;
-    zunpack<R>(lines + pr * L, L, k, X, Y);
+    zunpack<R>(lines + pr * LP, L, k, X, Y);
     if (c0 < a.ncols) a.cplx[(size_t)c0 * H + k] = X;
     if (c0 + 1 < a.ncols) a.cplx[(size_t)(c0 + 1) * H + k] = Y;
   }
@@ -628,6 +661,7 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_fz_r2c(FZArgs<R> a, co
 template <typename R, int L, int CP, int NT>
 __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_fz_c2r(FZArgs<R> a, const C2<R>* __restrict__ tw) {
   constexpr int H = L / 2 + 1;
+  constexpr int LP = zpad_len<R>(L);
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
   const int col0 = blockIdx.x * 2 * CP;
@@ -636,14 +670,14 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_fz_c2r(FZArgs<R> a, co
     const int c0 = col0 + 2 * pr;
     const C2<R> X = c0 < a.ncols ? a.cplx[(size_t)c0 * H + k] : czero<R>();
     const C2<R> Y = c0 + 1 < a.ncols ? a.cplx[(size_t)(c0 + 1) * H + k] : czero<R>();
-    zpack<R>(lines + pr * L, L, k, X, Y);
+    zpack<R>(lines + pr * LP, L, k, X, Y);
   }
   __syncthreads();
-  fft_smem<R, L, true, NT, CP, false>(lines, L, 1, tw);
+  fft_zlines<R, L, true, NT, CP>(lines, tw);
   for (int e = threadIdx.x; e < CP * L; e += NT) {
     const int pr = e / L, p = e % L;
     const int c0 = col0 + 2 * pr;
-    const C2<R> z = lines[pr * L + p];
+    const C2<R> z = lines[pr * LP + zi<R>(p)];
     if (c0 < a.ncols) a.real[(size_t)c0 * L + p] = z.x * a.scale;
     if (c0 + 1 < a.ncols) a.real[(size_t)(c0 + 1) * L + p] = z.y * a.scale;
   }

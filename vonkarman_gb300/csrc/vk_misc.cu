@@ -7,8 +7,8 @@ namespace vk {
 
 // One entry of EtdCoeffs::new (etd.rs:113-135) per integer |k|^2 index m:
 // lambda = -nu k^2, z = lambda dt.  The phi functions are the contour means
-// of etd.rs:15-84 with the shared exp(z + cos theta_j) factor evaluated once
-// per (z, j) for phi1, phi2 and phi3.
+// of etd.rs:15-84; exp(z + cos theta_j) is evaluated as exp(z) exp(cos theta_j)
+// (the second factor precomputed), shared by phi1, phi2 and phi3.
 __global__ void k_etd_table(double* __restrict__ tab, int nent, double nu, double ks2,
                             const DevScalars* __restrict__ d, int force, ContourConsts cc) {
   if (!force && d->etd_recompute == 0) return;
@@ -20,19 +20,20 @@ __global__ void k_etd_table(double* __restrict__ tab, int nent, double nu, doubl
   const double z = lambda * dt;
   const double zh = z / 2.0;
   double p1h = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
+  const double ez = exp(z), ezh = exp(zh);
   for (int j = 0; j < 32; ++j) {
     const double wim = cc.sth[j];
     // phi1(z/2)
     {
       const double wre = zh + cc.cth[j];
-      const double e = exp(wre);
+      const double e = ezh * cc.exp_cth[j];
       const double ere = e * cc.cos_sth[j], eim = e * cc.sin_sth[j];
       const double nre = ere - 1.0, nim = eim;
       const double den = wre * wre + wim * wim;
       p1h += (nre * wre + nim * wim) / den;
     }
     const double wre = z + cc.cth[j];
-    const double e = exp(wre);
+    const double e = ez * cc.exp_cth[j];
     const double ere = e * cc.cos_sth[j], eim = e * cc.sin_sth[j];
     {  // phi1(z)
       const double nre = ere - 1.0, nim = eim;
@@ -59,8 +60,8 @@ __global__ void k_etd_table(double* __restrict__ tab, int nent, double nu, doubl
   if (fabs(zh) < 1e-300) p1h = 1.0;
   if (fabs(z) < 1e-300) { p1 = 1.0; p2 = 0.5; p3 = 1.0 / 6.0; }
   double* t = tab + (size_t)m * ETD_STRIDE;
-  t[E_FULL] = exp(z);
-  t[E_HALF] = exp(zh);
+  t[E_FULL] = ez;
+  t[E_HALF] = ezh;
   t[E_A21] = p1h;
   t[E_A41] = p1;
   t[E_B1] = p1 - 3.0 * p2 + 4.0 * p3;

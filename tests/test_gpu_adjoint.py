@@ -43,6 +43,18 @@ def test_nonlinear_adjoint_vs_oracle(vk, n):
     assert nrel(vk.nonlinear_adjoint(s, x, nbar), want) < 1e-11
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("fp32bulk", 2e-5)])
+def test_nonlinear_adjoint_vs_oracle_n128(vk, precision, tol):
+    n = 128
+    g, ops, x = state(n)
+    nbar = vo.random_field(g, 6)
+    want = va.nonlinear_adjoint(ops, x, nbar)
+    s = vk.Periodic3D(vk.GridSpec(n), 0.05, x, vk.SolverOptions(precision=precision, dt_mode="fixed",
+                                                                  dt_fixed=0.02))
+    assert nrel(vk.nonlinear_adjoint(s, x, nbar), want) < tol
+    s.close()
+
+
 @pytest.mark.parametrize("n,nsteps,nsnap", [(8, 5, 5), (16, 3, 2), (16, 6, 1)])
 def test_gradient_vs_oracle(vk, n, nsteps, nsnap):
     g, ops, u0 = state(n)

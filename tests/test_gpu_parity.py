@@ -67,6 +67,22 @@ def test_fft_r2c_c2r_vs_numpy(vk, shape):
     f.close()
 
 
+# Every line length of the x / y passes (register-resident engine) and of the
+# z passes, in both precision forms: the 3/2-padded lengths up to M = 768
+# (N = 512) and the N-grid lengths up to 512.
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL64), ("fp32bulk", 1e-6)])
+@pytest.mark.parametrize("shape", [(768, 384, 8), (512, 256, 8), (192, 128, 8), (96, 48, 16), (32, 24, 12),
+                                   (16, 12, 8), (8, 64, 8), (8, 8, 768), (8, 8, 384), (8, 16, 512)])
+def test_fft_all_line_lengths_vs_numpy(vk, precision, tol, shape):
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(shape)
+    f = vk.GpuFftBackend(*shape, precision=precision)
+    ref = np.fft.rfftn(x)
+    assert nrel([f.r2c_3d(x)], [ref]) < tol
+    assert np.abs(f.c2r_3d(ref) - x).max() < 100 * tol * max(1.0, np.abs(x).max())
+    f.close()
+
+
 def test_fft_roundtrip_and_parseval_kats(vk):
     # ndrustfft_backend.rs:75-106 (roundtrip 1e-12) and :108-147 (Parseval 1e-10)
     n = 8
@@ -104,6 +120,34 @@ def test_nonlinear_vs_oracle(vk, n):
     got = vk.compute_nonlinear(s, u)
     assert nrel(got, want) < TOL64
     s.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL64), ("fp32bulk", TOL32)])
+def test_nonlinear_vs_oracle_n128(vk, precision, tol):
+    n = 128
+    g = vo.Grid(n)
+    u = random_state(n, 7)
+    want = vo.compute_nonlinear(vo.SpectralOps(g), u)
+    s = vk.Periodic3D(vk.GridSpec(n), 0.01, u, vk.SolverOptions(precision=precision, dt_mode="fixed",
+                                                                   dt_fixed=1e-3))
+    assert nrel(vk.compute_nonlinear(s, u), want) < tol
+    s.close()
+
+
+def test_nonlinear_fp32bulk_vs_fp64_n256(vk):
+    # M = 384 plans of both forms against each other (the oracle is too slow
+    # at this size): agreement to the FP32 level
+    from vonkarman_gb300 import ics
+
+    n = 256
+    u = ics.von_karman_isotropic(n, kp=4.0, energy=0.5, seed=5)
+    out = []
+    for prec in ("fp64", "fp32bulk"):
+        s = vk.Periodic3D(vk.GridSpec(n), 1e-3, u, vk.SolverOptions(precision=prec, dt_mode="fixed",
+                                                                      dt_fixed=1e-3))
+        out.append(vk.compute_nonlinear(s, u))
+        s.close()
+    assert nrel(out[1], out[0]) < TOL32
 
 
 def test_nonlinear_non_hermitian_input(vk):

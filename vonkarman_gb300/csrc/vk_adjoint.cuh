@@ -17,13 +17,13 @@
 //      accumulation of the adjoint ETD-RK4 step
 #pragma once
 
-#include "vk_kernels.cuh"
+#include "vk_lines.cuh"
 
 namespace vk {
 
 // A1: fields 0..4 as P1 on x; fields 5..7 = Pad(mul * S_out * P nbar / w_M).
 template <typename R> struct OpAdjXInv {
-  int nfields, nztiles, hz, nout;
+  int nfields, hz;
   int N, M;
   R s_in, s_cbar, ks;
   const C2<R>* in; size_t cs;          // stage input x
@@ -64,7 +64,7 @@ template <typename R> struct OpAdjXInv {
     }
     return cscale<R>(v, mul);
   }
-  __device__ __forceinline__ int src_pos(int i) const { return i; }
+  __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int iy, int z, int i, C2<R> v) const {
     out[(size_t)f * fs + ((size_t)i * N + iy) * hz + z] = v;
   }
@@ -73,14 +73,14 @@ template <typename R> struct OpAdjXInv {
 // A2: fields 0..5 as P2 (u, omega), fields 6..8 = y-inverse of c_bar.
 template <typename R> struct OpAdjYInv {
   OpYInv<R> base;   // reads input fields 0..4
-  int nfields, nztiles, hz, nout;
+  int nfields, hz;
   __device__ __forceinline__ C2<R> load(int f, int x, int z, int p) const {
     if (f < 6) return base.load(f, x, z, p);
     const int iy = unpad_pos(p, base.N, base.M);
     if (iy < 0) return czero<R>();
     return base.in[(size_t)(f - 1) * base.fsin + ((size_t)x * base.N + iy) * hz + z];
   }
-  __device__ __forceinline__ int src_pos(int i) const { return i; }
+  __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
     base.out[(size_t)f * base.fsout + ((size_t)x * base.M + i) * hz + z] = v;
   }
@@ -254,69 +254,79 @@ __device__ __forceinline__ void adj_stage_apply(const AdjStageArgs<R>& s, size_t
 // the o_bar part) / N^3, adjoint stage epilogue.  Shared memory: FFT tile plus
 // five finished fields.
 template <typename R> struct A5Args {
-  int N, M, H, nztiles;
+  int N, M, H, nlines;
   R s_out, ks;
   const C2<R>* in; size_t fsin;    // 6 fields (M, N, H)
   AdjStageArgs<R> st;
 };
 
-template <typename R, int L, int TZ, int NT>
-__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_adj_p5(A5Args<R> a, const C2<R>* __restrict__ tw) {
+template <typename R> struct A5Lines { static constexpr int value = sizeof(R) == 8 ? 4 : 8; };
+
+// Transposed P5 for the six cotangent fields (a_bar, o_bar): x-forward, keep
+// N of M modes, weight, and y = a_bar + i k x o_bar accumulated field by field
+// in shared memory (three accumulators; the thread producing output ix of a
+// field is the one that holds ix of every field, so the accumulation needs
+// no barrier), then the adjoint stage epilogue over the CTA's N x NLINES
+// modes.
+template <typename R, int L, int NLINES, int NT>
+__global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT, true>())
+k_adj_p5(A5Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int N = 2 * L / 3;
+  static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
   extern __shared__ __align__(16) unsigned char vk_smem[];
-  C2<R>* buf = reinterpret_cast<C2<R>*>(vk_smem);
-  C2<R>* keep = buf + L * TZ;
-  const int zt = blockIdx.x % a.nztiles;
-  const int iy = blockIdx.x / a.nztiles;
-  const int z0 = zt * TZ;
+  C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
+  C2<R>* acc = xb + rsmem_elems<R, L, NLINES>();   // 3 components x N x NLINES
   const int H = a.H;
-  constexpr int PER = (L * TZ + NT - 1) / NT;
-  for (int c = 0; c < 6; ++c) {
-    C2<R> ld[PER];
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int e = threadIdx.x + q * NT;
-      const int p = e / TZ, b = e % TZ;
-      const int z = z0 + b;
-      ld[q] = (e < L * TZ && z < H) ? a.in[(size_t)c * a.fsin + ((size_t)p * N + iy) * H + z] : czero<R>();
-    }
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int e = threadIdx.x + q * NT;
-      if (e < L * TZ) buf[e] = ld[q];
-    }
-    __syncthreads();
-    fft_smem<R, L, false, NT, TZ, true>(buf, 1, TZ, tw);
-    if (c == 5) break;
-    for (int e = threadIdx.x; e < N * TZ; e += NT) {
-      const int ix = e / TZ, b = e % TZ;
-      keep[c * N * TZ + e] = buf[pad_pos(ix, N, L) * TZ + b];
-    }
-    __syncthreads();
-  }
-  const int kyi = signed_k(iy, N);
-  const R ky = a.ks * (R)kyi;
-  for (int e = threadIdx.x; e < N * TZ; e += NT) {
-    const int ix = e / TZ, b = e % TZ;
-    const int z = z0 + b;
-    if (z >= H) continue;
-    const int kxi = signed_k(ix, N);
-    const R kx = a.ks * (R)kxi;
+  {
+    const int l = threadIdx.x % NLINES;
+    const int lam = blockIdx.x * NLINES + l;
+    const bool ok = lam < a.nlines;
+    const int iy = ok ? lam / H : 0;
+    const int z = ok ? lam - iy * H : 0;
+    const R ky = a.ks * (R)signed_k(iy, N);
     const R kz = a.ks * (R)z;
     const R wgt = a.s_out * (z == 0 ? R(1) : R(2));
-    C2<R> ab[3], ob[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) ab[c] = cscale<R>(keep[c * N * TZ + e], wgt);
-    ob[0] = cscale<R>(keep[3 * N * TZ + e], wgt);
-    ob[1] = cscale<R>(keep[4 * N * TZ + e], wgt);
-    ob[2] = cscale<R>(buf[pad_pos(ix, N, L) * TZ + b], wgt);
-    // y = ab + i k x ob  (spectral_ops.rs:92-104)
-    C2<R> y[3];
-    y[0] = cmk<R>(ab[0].x - (ky * ob[2].y - kz * ob[1].y), ab[0].y + (ky * ob[2].x - kz * ob[1].x));
-    y[1] = cmk<R>(ab[1].x - (kz * ob[0].y - kx * ob[2].y), ab[1].y + (kz * ob[0].x - kx * ob[2].x));
-    y[2] = cmk<R>(ab[2].x - (kx * ob[1].y - ky * ob[0].y), ab[2].y + (kx * ob[1].x - ky * ob[0].x));
-    const int m = kxi * kxi + kyi * kyi + z * z;
-    adj_stage_apply<R>(a.st, ((size_t)ix * N + iy) * H + z, m, y);
+    sfor<6>([&](auto cc) {
+      constexpr int C = decltype(cc)::value;
+      if (C > 0) __syncthreads();   // xb is reused
+      const C2<R>* src = a.in + (size_t)C * a.fsin + (size_t)iy * H + z;
+      fft_lines<R, L, false, NT, NLINES>(
+          xb, tw, [&](int, int p) { return ok ? src[(size_t)p * N * H] : czero<R>(); },
+          [&](int, int p, C2<R> v) {
+            const int ix = unpad_pos(p, N, L);
+            if (ix < 0) return;
+            v = cscale<R>(v, wgt);
+            C2<R>* y0 = acc + ix * NLINES + l;
+            C2<R>* y1 = y0 + N * NLINES;
+            C2<R>* y2 = y1 + N * NLINES;
+            const R kx = a.ks * (R)signed_k(ix, N);
+            // i k x o_bar (spectral_ops.rs:92-104), one o_bar component at a time
+            if constexpr (C < 3) {
+              (C == 0 ? *y0 : C == 1 ? *y1 : *y2) = v;
+            } else if constexpr (C == 3) {   // o_x: y_y += i kz o_x, y_z -= i ky o_x
+              *y1 = cadd<R>(*y1, cmul_i<R>(cscale<R>(v, kz)));
+              *y2 = csub<R>(*y2, cmul_i<R>(cscale<R>(v, ky)));
+            } else if constexpr (C == 4) {   // o_y: y_x -= i kz o_y, y_z += i kx o_y
+              *y0 = csub<R>(*y0, cmul_i<R>(cscale<R>(v, kz)));
+              *y2 = cadd<R>(*y2, cmul_i<R>(cscale<R>(v, kx)));
+            } else {                         // o_z: y_x += i ky o_z, y_y -= i kx o_z
+              *y0 = cadd<R>(*y0, cmul_i<R>(cscale<R>(v, ky)));
+              *y1 = csub<R>(*y1, cmul_i<R>(cscale<R>(v, kx)));
+            }
+          });
+    });
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int e = threadIdx.x; e < N * NLINES; e += NT) {
+    const int ix = e / NLINES, l = e % NLINES;
+    const int lam = blockIdx.x * NLINES + l;
+    if (lam >= a.nlines) continue;
+    const int iy = lam / H;
+    const int z = lam - iy * H;
+    const int kxi = signed_k(ix, N), kyi = signed_k(iy, N);
+    C2<R> y[3] = {acc[e], acc[N * NLINES + e], acc[2 * N * NLINES + e]};
+    adj_stage_apply<R>(a.st, ((size_t)ix * N + iy) * H + z, kxi * kxi + kyi * kyi + z * z, y);
   }
 }
 

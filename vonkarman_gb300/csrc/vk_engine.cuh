@@ -6,6 +6,7 @@
 #include <algorithm>
 
 #include "vk_adjoint.cuh"
+#include "vk_lines.cuh"
 #include "vk_reduce.cuh"
 
 namespace vk {
@@ -28,32 +29,33 @@ inline cudaError_t prepare_kernel(size_t smem) {
   return e;
 }
 
-// ---------------------------------------------------------------------------
-// Threads per strided CTA: one radix-8 butterfly per thread and stage in FP64
-// (bound by the FP64 pipe), two in FP32 (smaller CTAs, several per SM, so
-// load and compute phases of different CTAs overlap).
-template <typename R, int L, int TZ>
-__host__ __device__ constexpr int strided_nt() {
-  return cmax(64, cmin(1024, round32(TZ * L / max_radix<R>(L))));
+
+// Register-resident strided pass (k_lines): nouter * hz lines per field in
+// tiles of NLINES.
+template <typename R> struct NLof { static constexpr int value = 8; };
+template <typename R, int L> __host__ __device__ constexpr int lines_nt() {
+  return cmin(rthreads<R, L, NLof<R>::value>(), 384);
 }
 
-template <typename R, int L, bool INV, int TZ, class Op>
-inline cudaError_t launch_strided(const Op& op, int ntiles, const C2<R>* tw, cudaStream_t s) {
-  constexpr int NT = strided_nt<R, L, TZ>();
-  const size_t smem = (size_t)L * TZ * sizeof(C2<R>);
-  constexpr auto kern = k_strided<R, L, INV, TZ, NT, Op>;
+template <typename R, int L, bool INV, class Op>
+inline cudaError_t launch_lines(const Op& op, int nouter, const C2<R>* tw, cudaStream_t s) {
+  constexpr int NLINES = NLof<R>::value;
+  constexpr int NT = lines_nt<R, L>();
+  const size_t smem = (size_t)rsmem_elems<R, L, NLINES>() * sizeof(C2<R>);
+  constexpr auto kern = k_lines<R, L, INV, NLINES, NT, Op>;
   cudaError_t e = prepare_kernel<kern>(smem);
   if (e != cudaSuccess) return e;
-  kern<<<ntiles, NT, smem, s>>>(op, tw);
+  const int nlines = nouter * op.hz;
+  const int ntiles = (nlines + NLINES - 1) / NLINES;
+  kern<<<op.nfields * ntiles, NT, smem, s>>>(op, tw, nlines);
   return cudaGetLastError();
 }
+
 
 template <typename R, int N>
 inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   constexpr int M = 3 * N / 2;
   constexpr int H = N / 2 + 1;
-  constexpr int TZ = TZof<R>::value;
-  const int nzt = (H + TZ - 1) / TZ;
   const size_t fsA1 = (size_t)M * N * H;   // P1 out field stride
   const size_t fsB2 = (size_t)M * M * H;   // P2 out field stride
   const size_t fsA3 = (size_t)M * M * H;   // P3 out field stride
@@ -63,23 +65,23 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   // P1
   {
     TimerScope ts(p.timer, PASS_P1, s);
-    OpXInv<R> o{5, nzt, H, M, N, M, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fsA1};
-    e = launch_strided<R, M, true, TZ>(o, 5 * nzt * N, p.twM, s);
+    OpXInv<R> o{5, H, N, M, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fsA1};
+    e = launch_lines<R, M, true>(o, N, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   // P2
   {
     TimerScope ts(p.timer, PASS_P2, s);
-    OpYInv<R> o{6, nzt, H, M, N, M, 0, ks, p.bufA, fsA1, p.bufB, fsB2};
-    e = launch_strided<R, M, true, TZ>(o, 6 * nzt * M, p.twM, s);
+    OpYInv<R> o{6, H, N, M, 0, ks, p.bufA, fsA1, p.bufB, fsB2};
+    e = launch_lines<R, M, true>(o, M, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   // P3
   {
     TimerScope ts(p.timer, PASS_P3, s);
     constexpr int CP = zpairs<M, 384>();
-    constexpr int NT = zthreads<R, 6 * CP, M>();
-    const size_t smem = (size_t)6 * CP * zpad_len<R>(M) * sizeof(C2<R>);
+    constexpr int NT = p3_threads<R, M, CP>();
+    const size_t smem = (size_t)12 * CP * zpad_len<R>(M) * sizeof(C2<R>);
     constexpr auto kern = k_p3<R, M, CP, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
@@ -92,23 +94,24 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   // P4
   {
     TimerScope ts(p.timer, PASS_P4, s);
-    OpYFwdTrunc<R> o{3, nzt, H, N, N, M, p.bufA, fsA3, p.bufB, fsB4};
-    e = launch_strided<R, M, false, TZ>(o, 3 * nzt * M, p.twM, s);
+    OpYFwdTrunc<R> o{3, H, N, M, p.bufA, fsA3, p.bufB, fsB4};
+    e = launch_lines<R, M, false>(o, M, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   // P5
   {
     TimerScope ts(p.timer, PASS_P5, s);
-    constexpr int TZ5 = TZ / 2;
-    constexpr int NT = cmax(64, cmin(1024, round32(TZ5 * M / max_radix<R>(M))));
-    const int nzt5 = (H + TZ5 - 1) / TZ5;
-    const size_t smem = (size_t)(M + 2 * N) * TZ5 * sizeof(C2<R>);
-    constexpr auto kern = k_p5<R, M, TZ5, NT>;
+    constexpr int NL = P5Lines<R>::value;
+    constexpr int NT = cmin(rthreads<R, M, NL>(), 384);
+    const int nlines = N * H;
+    const size_t smem = (size_t)(rsmem_elems<R, M, NL>() + 3 * N * NL) * sizeof(C2<R>);
+    constexpr auto kern = k_p5<R, M, NL, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
     const double scale = (double)M * M * M / ((double)N * N * N);
-    P5Args<R> a{N, M, H, nzt5, (R)(1.0 / scale), ks, p.bufB, fsB4, p.st};
-    kern<<<nzt5 * N, NT, smem, s>>>(a, p.twM);
+    P5Args<R> a{N, M, H, nlines, (R)(1.0 / scale), ks, p.bufB, fsB4, p.st};
+    const int ntiles = (nlines + NL - 1) / NL;
+    kern<<<ntiles, NT, smem, s>>>(a, p.twM);
     e = cudaGetLastError();
   }
   return e;
@@ -118,8 +121,6 @@ template <typename R, int N>
 inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
   constexpr int M = 3 * N / 2;
   constexpr int H = N / 2 + 1;
-  constexpr int TZ = TZof<R>::value;
-  const int nzt = (H + TZ - 1) / TZ;
   const size_t fsA1 = (size_t)M * N * H;   // A1 out: 8 fields (M, N, H)
   const size_t fsB2 = (size_t)M * M * H;   // A2 out: 9 fields (M, M, H)
   const size_t fsA3 = (size_t)M * M * H;   // A3 out: 6 fields (M, M, H)
@@ -129,15 +130,15 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
   cudaError_t e;
   {
     TimerScope ts(p.timer, PASS_A1, s);
-    OpAdjXInv<R> o{8, nzt, H, M, N, M, (R)(1.0 / ((double)N * N * N)), (R)(1.0 / scale), ks,
+    OpAdjXInv<R> o{8, H, N, M, (R)(1.0 / ((double)N * N * N)), (R)(1.0 / scale), ks,
                    p.x, p.cs, p.nb, p.etd, p.slot, p.fac, p.dt, p.bufA, fsA1};
-    e = launch_strided<R, M, true, TZ>(o, 8 * nzt * N, p.twM, s);
+    e = launch_lines<R, M, true>(o, N, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   {
     TimerScope ts(p.timer, PASS_A2, s);
-    OpAdjYInv<R> o{OpYInv<R>{6, nzt, H, M, N, M, 0, ks, p.bufA, fsA1, p.bufB, fsB2}, 9, nzt, H, M};
-    e = launch_strided<R, M, true, TZ>(o, 9 * nzt * M, p.twM, s);
+    OpAdjYInv<R> o{OpYInv<R>{6, H, N, M, 0, ks, p.bufA, fsA1, p.bufB, fsB2}, 9, H};
+    e = launch_lines<R, M, true>(o, M, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   {
@@ -156,21 +157,22 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
   }
   {
     TimerScope ts(p.timer, PASS_A4, s);
-    OpYFwdTrunc<R> o{6, nzt, H, N, N, M, p.bufA, fsA3, p.bufB, fsB4};
-    e = launch_strided<R, M, false, TZ>(o, 6 * nzt * M, p.twM, s);
+    OpYFwdTrunc<R> o{6, H, N, M, p.bufA, fsA3, p.bufB, fsB4};
+    e = launch_lines<R, M, false>(o, M, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   {
     TimerScope ts(p.timer, PASS_A5, s);
-    constexpr int TZ5 = (sizeof(R) == 8 && M >= 768) ? 2 : TZ / 2;
-    constexpr int NT = cmax(64, cmin(1024, round32(TZ5 * M / max_radix<R>(M))));
-    const int nzt5 = (H + TZ5 - 1) / TZ5;
-    const size_t smem = (size_t)(M + 5 * N) * TZ5 * sizeof(C2<R>);
-    constexpr auto kern = k_adj_p5<R, M, TZ5, NT>;
+    constexpr int NL = A5Lines<R>::value;
+    constexpr int NT = cmin(rthreads<R, M, NL>(), 384);
+    const int nlines = N * H;
+    const size_t smem = (size_t)(rsmem_elems<R, M, NL>() + 3 * N * NL) * sizeof(C2<R>);
+    constexpr auto kern = k_adj_p5<R, M, NL, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
-    A5Args<R> a{N, M, H, nzt5, (R)(1.0 / ((double)N * N * N)), ks, p.bufB, fsB4, p.st};
-    kern<<<nzt5 * N, NT, smem, s>>>(a, p.twM);
+    A5Args<R> a{N, M, H, nlines, (R)(1.0 / ((double)N * N * N)), ks, p.bufB, fsB4, p.st};
+    const int ntiles = (nlines + NL - 1) / NL;
+    kern<<<ntiles, NT, smem, s>>>(a, p.twM);
     e = cudaGetLastError();
   }
   return e;
@@ -179,8 +181,6 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
 template <typename R, int N>
 inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
   constexpr int H = N / 2 + 1;
-  constexpr int TZ = TZof<R>::value;
-  const int nzt = (H + TZ - 1) / TZ;
   const size_t fs = (size_t)N * N * H;
   const R ks = (R)p.ks;
   const bool both = p.which == 3;
@@ -189,16 +189,16 @@ inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
   {
     TimerScope ts(p.timer, PASS_NX, s);
     const int nf = need_w ? 5 : 3;
-    OpXInv<R> o{nf, nzt, H, N, N, N, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fs};
-    e = launch_strided<R, N, true, TZ>(o, nf * nzt * N, p.twN, s);
+    OpXInv<R> o{nf, H, N, N, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fs};
+    e = launch_lines<R, N, true>(o, N, p.twN, s);
     if (e != cudaSuccess) return e;
   }
   {
     TimerScope ts(p.timer, PASS_NY, s);
     const int nf = both ? 6 : 3;
     const int gbase = p.which == 2 ? 3 : 0;
-    OpYInv<R> o{nf, nzt, H, N, N, N, gbase, ks, p.bufA, fs, p.bufB, fs};
-    e = launch_strided<R, N, true, TZ>(o, nf * nzt * N, p.twN, s);
+    OpYInv<R> o{nf, H, N, N, gbase, ks, p.bufA, fs, p.bufB, fs};
+    e = launch_lines<R, N, true>(o, N, p.twN, s);
     if (e != cudaSuccess) return e;
   }
   TimerScope ts(p.timer, PASS_NZ, s);
@@ -249,14 +249,12 @@ inline cudaError_t fz_pass(const FftParams<R>& p, bool inverse, R scale, cudaStr
 
 template <typename R, int L, int AXIS>
 inline cudaError_t fxy_pass(const FftParams<R>& p, bool inverse, cudaStream_t s) {
-  constexpr int TZ = TZof<R>::value;
   const int hz = p.nz / 2 + 1;
-  const int nzt = (hz + TZ - 1) / TZ;
-  OpPlainC2C<R, AXIS> o{1, nzt, hz, L, p.nx, p.ny, p.cplx};
+  OpPlainC2C<R, AXIS> o{1, hz, p.nx, p.ny, p.cplx};
   const int nouter = AXIS == 0 ? p.ny : p.nx;
   const C2<R>* tw = AXIS == 0 ? p.twx : p.twy;
-  if (inverse) return launch_strided<R, L, true, TZ>(o, nzt * nouter, tw, s);
-  return launch_strided<R, L, false, TZ>(o, nzt * nouter, tw, s);
+  if (inverse) return launch_lines<R, L, true>(o, nouter, tw, s);
+  return launch_lines<R, L, false>(o, nouter, tw, s);
 }
 
 #define VK_FOR_LENGTHS(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(12) X(24) X(48) X(96) X(192) X(384) X(768)

@@ -13,6 +13,9 @@
 // (vonkarman-fft/src/ndrustfft_backend.rs:46-57) into their load/store steps.
 #pragma once
 
+#include <type_traits>
+#include <utility>
+
 #include "vk_host.h"
 
 namespace vk {
@@ -284,9 +287,123 @@ __device__ __forceinline__ void rad16(C2<R>* v, const C2<R>* w) {
   v[3] = x[0]; v[7] = x[1]; v[11] = x[2]; v[15] = x[3];
 }
 
+// ---------------------------------------------------------------------------
+// Compile-time twiddles for the composite radices: cos and sin of 2 pi m / n
+// from Taylor series on [0, pi/4] after an exact octant reduction in integers.
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr double ct_sin_red(double x) {
+  double term = x, sum = x;
+  for (int k = 1; k < 14; ++k) {
+    term *= -x * x / (double)((2 * k) * (2 * k + 1));
+    sum += term;
+  }
+  return sum;
+}
+__host__ __device__ constexpr double ct_cos_red(double x) {
+  double term = 1.0, sum = 1.0;
+  for (int k = 1; k < 14; ++k) {
+    term *= -x * x / (double)((2 * k - 1) * (2 * k));
+    sum += term;
+  }
+  return sum;
+}
+// (cos, sin)(2 pi m / n): angle = (pi/4) (oct + rem/n) with oct = 8m div n
+__host__ __device__ constexpr double ct_trig(int m, int n, bool want_sin) {
+  const double quarter_pi = 0.78539816339744830961566084581987572;
+  m %= n;
+  if (m < 0) m += n;
+  const long long t = 8LL * m;
+  int oct = (int)(t / n);
+  const long long rem = t - (long long)oct * n;
+  double c = 0.0, s = 0.0;
+  int q = 0;
+  if (oct % 2 == 0) {           // q quarter turns + phi, phi in [0, pi/4)
+    const double phi = quarter_pi * (double)rem / (double)n;
+    c = ct_cos_red(phi);
+    s = ct_sin_red(phi);
+    q = oct / 2;
+  } else {                      // q quarter turns - psi, psi in (0, pi/4]
+    const double psi = quarter_pi * (double)(n - rem) / (double)n;
+    c = ct_cos_red(psi);
+    s = -ct_sin_red(psi);
+    q = (oct + 1) / 2;
+  }
+  double rc = c, rs = s;        // rotate (c, s) by q quarter turns
+  if (q % 4 == 1) { rc = -s; rs = c; }
+  if (q % 4 == 2) { rc = -c; rs = -s; }
+  if (q % 4 == 3) { rc = s; rs = -c; }
+  return want_sin ? rs : rc;
+}
+// forward twiddle W_n^m = exp(-2 pi i m / n) as a compile-time constant
+template <int M, int NN> struct CTw {
+  static constexpr double c = ct_trig(M, NN, false);
+  static constexpr double s = -ct_trig(M, NN, true);
+};
+
+// Compile-time loop: f(std::integral_constant<int, i>) for i = 0..N-1.
+template <class F, int... I>
+__device__ __forceinline__ void sfor_impl(F&& f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, class F>
+__device__ __forceinline__ void sfor(F&& f) {
+  sfor_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+template <typename R, bool INV, int RAD, bool TW>
+__device__ __forceinline__ void dft(C2<R>* v, const C2<R>* w);
+
+// Composite radix RAD = A * B in registers (Cooley-Tukey): n = b + B a,
+// k = kA + A kB.  A-point DFTs over a (stage twiddles fused), then B-point
+// DFTs over b with the internal twiddles W_RAD^(b kA) fused.
+template <int RAD> __host__ __device__ constexpr int comp_a() {
+  return RAD == 6 ? 3 : RAD == 12 ? 4 : RAD == 24 ? 8 : RAD == 32 ? 8 : RAD == 48 ? 16 : 0;
+}
+
+template <typename R, bool INV, int RAD, bool TW>
+__device__ __forceinline__ void dft_comp(C2<R>* v, const C2<R>* w) {
+  constexpr int A = comp_a<RAD>();
+  constexpr int B = RAD / A;
+  static_assert(A > 0 && A * B == RAD, "unsupported composite radix");
+  C2<R> y[B][A];
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    C2<R> t[A], tw[A];
+#pragma unroll
+    for (int a = 0; a < A; ++a) t[a] = v[b + B * a];
+    if (TW) {
+#pragma unroll
+      for (int a = 1; a < A; ++a) tw[a] = w[b + B * a];
+      if (b > 0) t[0] = tw_mul<R, INV>(w[b], t[0]);
+    }
+    dft<R, INV, A, TW>(t, tw);
+#pragma unroll
+    for (int k = 0; k < A; ++k) y[b][k] = t[k];
+  }
+  sfor<A>([&](auto kac) {
+    constexpr int KA = decltype(kac)::value;
+    C2<R> t[B], tw[B];
+#pragma unroll
+    for (int b = 0; b < B; ++b) t[b] = y[b][KA];
+    if constexpr (KA == 0) {
+      dft<R, INV, B, false>(t, tw);
+    } else {
+      sfor<B>([&](auto bc) {
+        constexpr int BB = decltype(bc)::value;
+        tw[BB] = cmk<R>((R)CTw<BB * KA, RAD>::c, (R)CTw<BB * KA, RAD>::s);
+      });
+      dft<R, INV, B, true>(t, tw);
+    }
+#pragma unroll
+    for (int k = 0; k < B; ++k) v[KA + A * k] = t[k];
+  });
+}
+
 template <typename R, bool INV, int RAD, bool TW>
 __device__ __forceinline__ void dft(C2<R>* v, const C2<R>* w) {
-  if constexpr (RAD == 16) {
+  if constexpr (comp_a<RAD>() > 0) {
+    dft_comp<R, INV, RAD, TW>(v, w);
+  } else if constexpr (RAD == 16) {
     rad16<R, INV, TW>(v, w);
   } else if constexpr (RAD == 8) {
     rad8<R, INV, TW>(v, w);

@@ -43,10 +43,6 @@ __host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 __host__ __device__ constexpr int round32(int a) { return (a + 31) / 32 * 32; }
 
-// Lines per CTA for the strided (x / y) passes: TZ = 8 consecutive iz values
-// (128-byte row segments in FP64, 64 in FP32; small FP32 tiles let several
-// CTAs per SM overlap their load and compute phases).
-template <typename R> struct TZof { static constexpr int value = 8; };
 // z passes: column pairs per CTA so that CP * L == 768 (z-cross) / 512 (N grid)
 template <int L, int TARGET> __host__ __device__ constexpr int zpairs() { return cmax(1, TARGET / L); }
 template <typename R, int NLINES, int L>
@@ -55,52 +51,12 @@ __host__ __device__ constexpr int zthreads() { return cmax(64, cmin(1024, round3
 // warps per SM, which caps registers near 85 per thread.
 template <int NT> __host__ __device__ constexpr int min_blocks() { return cmax(1, 768 / NT); }
 
-// ---------------------------------------------------------------------------
-// Generic strided pass: one field of TZ interleaved lines per CTA.
-// blockIdx.x = f + nfields * (ztile + nztiles * outer).  All loads of a CTA
-// are issued into registers before the first shared-memory store, so each
-// thread has PER loads in flight.
-// ---------------------------------------------------------------------------
-template <typename R, int L, bool INV, int TZ, int NT, class Op>
-__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_strided(Op op, const C2<R>* __restrict__ tw) {
-  extern __shared__ __align__(16) unsigned char vk_smem[];
-  C2<R>* buf = reinterpret_cast<C2<R>*>(vk_smem);
-  constexpr int PER = (L * TZ + NT - 1) / NT;
-  const int f = blockIdx.x % op.nfields;
-  const int rest = blockIdx.x / op.nfields;
-  const int z0 = (rest % op.nztiles) * TZ;
-  const int outer = rest / op.nztiles;
-  C2<R> ld[PER];
-#pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int e = threadIdx.x + q * NT;
-    ld[q] = czero<R>();
-    if (e < L * TZ) {
-      const int p = e / TZ, b = e % TZ;
-      const int z = z0 + b;
-      if (z < op.hz) ld[q] = op.load(f, outer, z, p);
-    }
-  }
-#pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int e = threadIdx.x + q * NT;
-    if (e < L * TZ) buf[e] = ld[q];
-  }
-  __syncthreads();
-  fft_smem<R, L, INV, NT, TZ, true>(buf, 1, TZ, tw);
-  for (int e = threadIdx.x; e < op.nout * TZ; e += NT) {
-    const int i = e / TZ, b = e % TZ;
-    const int z = z0 + b;
-    if (z < op.hz) op.store(f, outer, z, i, buf[op.src_pos(i) * TZ + b]);
-  }
-}
-
 // P1 / N-grid X: x-inverse of the spectral state, zero-pad N -> M (M == N on
 // the N grid).  Fields: 0..2 = u_c, 3 = i kx u_y, 4 = i kx u_z.  s_in folds the
 // 1/M^3 of the padded c2r and the (M/N)^3 pre-scale (dealiased.rs:43,:45-62)
 // into one factor 1/N^3.
 template <typename R> struct OpXInv {
-  int nfields, nztiles, hz, nout;
+  int nfields, hz;
   int N, M;
   R s_in, ks;
   const C2<R>* in; size_t cs;
@@ -117,7 +73,7 @@ template <typename R> struct OpXInv {
     }
     return v;
   }
-  __device__ __forceinline__ int src_pos(int i) const { return i; }
+  __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int iy, int z, int i, C2<R> v) const {
     out[(size_t)f * fs + ((size_t)i * N + iy) * hz + z] = v;
   }
@@ -128,7 +84,7 @@ template <typename R> struct OpXInv {
 // (curl: vonkarman-core/src/spectral_ops.rs:81-108).  kx was applied in P1, ky
 // and kz are applied here (both are constant along an x line).
 template <typename R> struct OpYInv {
-  int nfields, nztiles, hz, nout;
+  int nfields, hz;
   int N, M, gbase;
   R ks;
   const C2<R>* in; size_t fsin;   // (M, N, H): Ux, Uy, Uz, Vy, Vz
@@ -154,7 +110,7 @@ template <typename R> struct OpYInv {
     const C2<R> ux = in[base], vy = in[3 * fsin + base];
     return cmk<R>(vy.x + ky * ux.y, vy.y - ky * ux.x);
   }
-  __device__ __forceinline__ int src_pos(int i) const { return i; }
+  __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
     out[(size_t)f * fsout + ((size_t)x * M + i) * hz + z] = v;
   }
@@ -163,14 +119,14 @@ template <typename R> struct OpYInv {
 // P4: y-forward of the three cross-product fields, keep N of M modes
 // (truncate_spectral, dealiased.rs:141-163).
 template <typename R> struct OpYFwdTrunc {
-  int nfields, nztiles, hz, nout;
+  int nfields, hz;
   int N, M;
   const C2<R>* in; size_t fsin;   // (M, M, H)
   C2<R>* out; size_t fsout;       // (M, N, H)
   __device__ __forceinline__ C2<R> load(int f, int x, int z, int p) const {
     return in[(size_t)f * fsin + ((size_t)x * M + p) * hz + z];
   }
-  __device__ __forceinline__ int src_pos(int i) const { return pad_pos(i, N, M); }
+  __device__ __forceinline__ int out_index(int p) const { return unpad_pos(p, N, M); }
   __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
     out[(size_t)f * fsout + ((size_t)x * N + i) * hz + z] = v;
   }
@@ -179,14 +135,14 @@ template <typename R> struct OpYFwdTrunc {
 // Standalone FFT backend: C2C along x (AXIS 0) or y (AXIS 1) of an
 // (nx, ny, hz) complex array, in place.
 template <typename R, int AXIS> struct OpPlainC2C {
-  int nfields, nztiles, hz, nout;
+  int nfields, hz;
   int nx, ny;
   C2<R>* data;
   __device__ __forceinline__ size_t at(int outer, int z, int p) const {
     return AXIS == 0 ? ((size_t)p * ny + outer) * hz + z : ((size_t)outer * ny + p) * hz + z;
   }
   __device__ __forceinline__ C2<R> load(int, int outer, int z, int p) const { return data[at(outer, z, p)]; }
-  __device__ __forceinline__ int src_pos(int i) const { return i; }
+  __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int, int outer, int z, int i, C2<R> v) const { data[at(outer, z, i)] = v; }
 };
 
@@ -300,78 +256,6 @@ __device__ __forceinline__ void stage_apply(const StageArgs<R>& s, size_t idx, i
   }
 }
 
-// ---------------------------------------------------------------------------
-// P5: x-forward of the three fields, keep N of M modes, scale by N^3/M^3
-// (dealiased.rs:102-109), Leray projection (spectral_ops.rs:114-151), stage
-// epilogue.  One CTA = one iy and TZ consecutive iz, all three components;
-// shared memory holds the FFT tile (L x TZ) plus two finished components
-// (2 x N x TZ).
-// ---------------------------------------------------------------------------
-template <typename R> struct P5Args {
-  int N, M, H, nztiles;
-  R s_out, ks;
-  const C2<R>* in; size_t fsin;   // (M, N, H)
-  StageArgs<R> st;
-};
-
-template <typename R, int L, int TZ, int NT>
-__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
-  constexpr int N = 2 * L / 3;
-  extern __shared__ __align__(16) unsigned char vk_smem[];
-  C2<R>* buf = reinterpret_cast<C2<R>*>(vk_smem);
-  C2<R>* keep = buf + L * TZ;
-  const int zt = blockIdx.x % a.nztiles;
-  const int iy = blockIdx.x / a.nztiles;
-  const int z0 = zt * TZ;
-  const int H = a.H;
-  constexpr int PER = (L * TZ + NT - 1) / NT;
-  for (int c = 0; c < 3; ++c) {
-    C2<R> ld[PER];
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int e = threadIdx.x + q * NT;
-      const int p = e / TZ, b = e % TZ;
-      const int z = z0 + b;
-      ld[q] = (e < L * TZ && z < H) ? a.in[(size_t)c * a.fsin + ((size_t)p * N + iy) * H + z] : czero<R>();
-    }
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int e = threadIdx.x + q * NT;
-      if (e < L * TZ) buf[e] = ld[q];
-    }
-    __syncthreads();
-    fft_smem<R, L, false, NT, TZ, true>(buf, 1, TZ, tw);
-    if (c == 2) break;  // the third field stays in buf
-    for (int e = threadIdx.x; e < N * TZ; e += NT) {
-      const int ix = e / TZ, b = e % TZ;
-      keep[c * N * TZ + e] = buf[pad_pos(ix, N, L) * TZ + b];
-    }
-    __syncthreads();
-  }
-  const int kyi = signed_k(iy, N);
-  const R ky = a.ks * (R)kyi;
-  for (int e = threadIdx.x; e < N * TZ; e += NT) {
-    const int ix = e / TZ, b = e % TZ;
-    const int z = z0 + b;
-    if (z >= H) continue;
-    const int kxi = signed_k(ix, N);
-    const R kx = a.ks * (R)kxi;
-    const R kz = a.ks * (R)z;
-    C2<R> nl[3] = {cscale<R>(keep[e], a.s_out), cscale<R>(keep[N * TZ + e], a.s_out),
-                   cscale<R>(buf[pad_pos(ix, N, L) * TZ + b], a.s_out)};
-    const R k2 = (kx * kx + ky * ky) + kz * kz;
-    if (!(k2 < R(1e-30))) {
-      const R inv = R(1) / k2;
-      const C2<R> kd = cmk<R>((kx * nl[0].x + ky * nl[1].x) + kz * nl[2].x,
-                              (kx * nl[0].y + ky * nl[1].y) + kz * nl[2].y);
-      nl[0] = cmk<R>(nl[0].x - kx * kd.x * inv, nl[0].y - kx * kd.y * inv);
-      nl[1] = cmk<R>(nl[1].x - ky * kd.x * inv, nl[1].y - ky * kd.y * inv);
-      nl[2] = cmk<R>(nl[2].x - kz * kd.x * inv, nl[2].y - kz * kd.y * inv);
-    }
-    const int m = kxi * kxi + kyi * kyi + z * z;
-    stage_apply<R>(a.st, ((size_t)ix * N + iy) * H + z, m, k2, nl);
-  }
-}
 
 // ---------------------------------------------------------------------------
 // z-line helpers.  Two real z lines x, y of length L share one complex line
@@ -413,98 +297,6 @@ template <typename R> struct P3Args {
   const C2<R>* in; size_t fsin;     // 6 fields (M, M, H)
   C2<R>* out; size_t fsout;         // 3 fields (M, M, H)
 };
-
-template <typename R, int M, int CP, int NT>
-__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
-  constexpr int N = 2 * M / 3;
-  constexpr int H = N / 2 + 1;
-  constexpr int NL = 6 * CP;
-  constexpr int LP = zpad_len<R>(M);
-  extern __shared__ __align__(16) unsigned char vk_smem[];
-  C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
-  const int col0 = blockIdx.x * 2 * CP;
-  // load + pack (all loads of a thread issued before the packing stores)
-  constexpr int TOT = 2 * CP * 3 * H;
-  constexpr int PER = (TOT + NT - 1) / NT;
-  C2<R> lx[PER], ly[PER];
-#pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int e = threadIdx.x + q * NT;
-    const int k = e % H;
-    const int t = (e / H) % 3;
-    const int col = col0 + e / (3 * H);
-    const bool ok = e < TOT && col < a.ncols;
-    lx[q] = ok ? a.in[(size_t)(2 * t) * a.fsin + (size_t)col * H + k] : czero<R>();
-    ly[q] = ok ? a.in[(size_t)(2 * t + 1) * a.fsin + (size_t)col * H + k] : czero<R>();
-  }
-#pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int e = threadIdx.x + q * NT;
-    if (e < TOT) {
-      const int k = e % H;
-      const int t = (e / H) % 3;
-      const int cr = e / (3 * H);
-      zpack<R>(lines + (6 * (cr / 2) + 3 * (cr % 2) + t) * LP, M, k, lx[q], ly[q]);
-    }
-  }
-  for (int e = threadIdx.x; e < NL * (N / 2 - 1); e += NT) {
-    const int l = e / (N / 2 - 1), p = H + e % (N / 2 - 1);
-    lines[l * LP + zi<R>(p)] = czero<R>();
-  }
-  __syncthreads();
-  fft_zlines<R, M, true, NT, NL>(lines, tw);
-  // cross product, two phases (all reads, sync, all writes)
-  constexpr int QX = (CP * M + NT - 1) / NT;
-  C2<R> res[QX][3];
-#pragma unroll
-  for (int q = 0; q < QX; ++q) {
-    const int e = threadIdx.x + q * NT;
-    if (e < CP * M) {
-      const int pr = e / M, p = e % M;
-      R cz[2];
-#pragma unroll
-      for (int cc = 0; cc < 2; ++cc) {
-        const C2<R>* L0 = lines + (6 * pr + 3 * cc) * LP;
-        const C2<R> A = L0[zi<R>(p)], B = L0[LP + zi<R>(p)], C = L0[2 * LP + zi<R>(p)];
-        const R ux = A.x, uy = A.y, uz = B.x, wx = B.y, wy = C.x, wz = C.y;
-        res[q][cc] = cmk<R>(uy * wz - uz * wy, uz * wx - ux * wz);
-        cz[cc] = ux * wy - uy * wx;
-      }
-      res[q][2] = cmk<R>(cz[0], cz[1]);
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < QX; ++q) {
-    const int e = threadIdx.x + q * NT;
-    if (e < CP * M) {
-      const int pr = e / M, p = e % M;
-#pragma unroll
-      for (int j = 0; j < 3; ++j) lines[(3 * pr + j) * LP + zi<R>(p)] = res[q][j];
-    }
-  }
-  __syncthreads();
-  fft_zlines<R, M, false, NT, 3 * CP>(lines, tw);
-  // unpack + store H modes of c_x, c_y, c_z for both columns of each pair
-  for (int e = threadIdx.x; e < CP * 3 * H; e += NT) {
-    const int k = e % H;
-    const int j = (e / H) % 3;
-    const int pr = e / (3 * H);
-    C2<R> X, Y;
-    zunpack<R>(lines + (3 * pr + j) * LP, M, k, X, Y);
-    const int c0 = col0 + 2 * pr;
-    if (j < 2) {
-      const int col = c0 + j;
-      if (col < a.ncols) {
-        a.out[(size_t)col * H + k] = X;
-        a.out[a.fsout + (size_t)col * H + k] = Y;
-      }
-    } else {
-      if (c0 < a.ncols) a.out[2 * a.fsout + (size_t)c0 * H + k] = X;
-      if (c0 + 1 < a.ncols) a.out[2 * a.fsout + (size_t)(c0 + 1) * H + k] = Y;
-    }
-  }
-}
 
 // ---------------------------------------------------------------------------
 // N-grid z pass: c2r of u and/or omega (already x/y-inverted and scaled by

@@ -1,0 +1,365 @@
+// Register-resident batched line FFT for the strided (x / y) passes.
+//
+// NLINES interleaved lines of length L are transformed by a Stockham
+// auto-sort whose stages live in registers: the first stage reads its
+// butterfly inputs straight from global memory (through the pass's load
+// functor, which also applies zero-padding and derivative factors), every
+// later stage reads them from a shared-memory exchange buffer written by the
+// stage before, and the last stage hands its outputs straight to the pass's
+// store functor (which applies truncation).  With the FP32 plans (two stages
+// for every padded length up to 768) each element crosses shared memory once.
+//
+// Thread g handles butterfly j = g / NLINES of line l = g % NLINES in every
+// stage, so consecutive lanes take consecutive lines: with the lines
+// consecutive in memory (z fastest) global accesses are row segments of
+// NLINES elements.
+#pragma once
+
+#include "vk_kernels.cuh"
+
+namespace vk {
+
+// FP32 plans: at most two stages up to L = 768, composite in-register radices
+// 6/12/24/32; the larger radix goes first, where it carries no twiddles.  FP64 plans: radix <= 8 (register budget), as in the
+// shared-memory engine.
+__host__ __device__ constexpr int rplan_stages_f(int L) {
+  return (L == 8 || L == 12 || L == 16 || L == 24) ? 1
+       : (L == 32 || L == 48 || L == 64 || L == 96 || L == 128 || L == 192 || L == 256 || L == 384 || L == 512 || L == 768) ? 2
+       : -1;
+}
+__host__ __device__ constexpr int rplan_radix_f(int L, int s) {
+  return L <= 24 ? L
+       : L == 32 ? (s == 0 ? 8 : 4)
+       : L == 48 ? (s == 0 ? 16 : 3)
+       : L == 64 ? (s == 0 ? 16 : 4)
+       : L == 96 ? (s == 0 ? 16 : 6)
+       : L == 128 ? (s == 0 ? 16 : 8)
+       : L == 192 ? (s == 0 ? 16 : 12)
+       : L == 256 ? 16
+       : L == 384 ? (s == 0 ? 24 : 16)
+       : L == 512 ? (s == 0 ? 32 : 16)
+       : L == 768 ? (s == 0 ? 32 : 24)
+       : 1;
+}
+template <typename R> __host__ __device__ constexpr int rstages(int L) {
+  return sizeof(R) == 4 ? rplan_stages_f(L) : plan_stages(L);
+}
+template <typename R> __host__ __device__ constexpr int rradix(int L, int s) {
+  return sizeof(R) == 4 ? rplan_radix_f(L, s) : plan_radix(L, s);
+}
+// threads of a CTA: one butterfly per thread in the widest stage
+template <typename R, int L, int NLINES, int S = 0>
+__host__ __device__ constexpr int rthreads() {
+  if constexpr (S >= rstages<R>(L)) {
+    return 32;
+  } else {
+    return cmax(round32(L / rradix<R>(L, S) * NLINES), rthreads<R, L, NLINES, S + 1>());
+  }
+}
+// FP32 with 8 lines: the first stage writes at stride RAD0 positions, so a
+// padding slot after every RAD0 positions spreads a warp over both halves of
+// the 32 banks.  FP64 rows of 8 lines are already 128 bytes.
+template <typename R, int L, int NLINES>
+__host__ __device__ constexpr bool rpad() { return sizeof(R) == 4 && NLINES < 16 && rstages<R>(L) > 1; }
+template <typename R, int L, int NLINES>
+__host__ __device__ constexpr int rsmem_elems() {
+  return rstages<R>(L) > 1 ? (L + (rpad<R, L, NLINES>() ? L / rradix<R>(L, 0) : 0)) * NLINES : 0;
+}
+template <typename R, int L, int NLINES, int S>
+__device__ __forceinline__ int ridx(int pos, int l) {
+  if constexpr (S == 0 && rpad<R, L, NLINES>()) {
+    return (pos + pos / rradix<R>(L, 0)) * NLINES + l;
+  } else {
+    return pos * NLINES + l;
+  }
+}
+
+// Minimum resident CTAs per SM requested from the compiler (caps registers):
+// 24 warps per SM for the strided passes where the plan allows it; one or two
+// CTAs for the long FP64 / 768-point plans and for the multi-field P5 kernels
+// (EPI), whose shared memory limits residency anyway.
+template <typename R, int L, int NT, bool EPI = false>
+__host__ __device__ constexpr int lines_min_blocks() {
+  if constexpr (sizeof(R) == 8) {
+    return L >= 512 ? 1 : cmax(1, 768 / NT);
+  } else {
+    return L >= 768 ? (EPI ? 1 : 2) : EPI ? cmax(1, 512 / NT) : NT < 128 ? 4 : cmax(1, 768 / NT);
+  }
+}
+
+// Thread-to-butterfly maps and exchange layouts.
+// Interleaved lines (x / y passes, element p of line l at p * NLINES + l):
+// consecutive lanes take consecutive lines, so every thread keeps one line.
+template <typename R, int L, int NLINES>
+struct MapInterleaved {
+  template <int NB> __device__ __forceinline__ static int line(int g) { return g % NLINES; }
+  template <int NB> __device__ __forceinline__ static int bfly(int g) { return g / NLINES; }
+  template <int S> __device__ __forceinline__ static int idx(int pos, int l) { return ridx<R, L, NLINES, S>(pos, l); }
+  static constexpr int elems() { return rsmem_elems<R, L, NLINES>(); }
+};
+// Contiguous lines (z passes, element p of line l at l * LP + zi(p), one
+// padding slot per 128 bytes): consecutive lanes take consecutive
+// butterflies of a line, so global accesses along a line coalesce.
+template <typename R, int L, int NLINES>
+struct MapContig {
+  template <int NB> __device__ __forceinline__ static int line(int g) { return g / NB; }
+  template <int NB> __device__ __forceinline__ static int bfly(int g) { return g % NB; }
+  template <int S> __device__ __forceinline__ static int idx(int pos, int l) { return l * zpad_len<R>(L) + zi<R>(pos); }
+  static constexpr int elems() { return NLINES * zpad_len<R>(L); }
+};
+
+template <typename R, int L, bool INV, int NT, int NLINES, class MAP, int S, int NS>
+struct RegStage {
+  static constexpr int RAD = rradix<R>(L, S);
+  static constexpr int NB = L / RAD;            // butterflies per line
+  static constexpr int G = NB * NLINES;         // butterflies per stage
+  static constexpr int Q = (G + NT - 1) / NT;
+  static constexpr bool LAST = S + 1 == rstages<R>(L);
+  static constexpr int TWS = L / (NS * RAD);    // twiddle table stride
+
+  // ld(l, p) -> input position p of line l; st(l, p, v) takes output p.
+  template <class LD, class ST>
+  __device__ __forceinline__ static void run(C2<R>* xb, const C2<R>* __restrict__ tw, const LD& ld,
+                                             const ST& st) {
+    const int tid = threadIdx.x;
+    C2<R> v[Q][RAD];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int g = tid + q * NT;
+      if (G % NT == 0 || g < G) {
+        const int l = MAP::template line<NB>(g);
+        const int j = MAP::template bfly<NB>(g);
+        if constexpr (S == 0) {
+#pragma unroll
+          for (int r = 0; r < RAD; ++r) v[q][r] = ld(l, j + r * NB);
+        } else {
+#pragma unroll
+          for (int r = 0; r < RAD; ++r) v[q][r] = xb[MAP::template idx<S - 1>(j + r * NB, l)];
+        }
+      }
+    }
+    // a later stage writes the buffer it has just read: wait for all readers
+    if constexpr (S > 0 && !LAST) __syncthreads();
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int g = tid + q * NT;
+      if (G % NT == 0 || g < G) {
+        const int l = MAP::template line<NB>(g);
+        const int j = MAP::template bfly<NB>(g);
+        const int k = j % NS;
+        C2<R> w[RAD];
+        if constexpr (S > 0) {
+#pragma unroll
+          for (int r = 1; r < RAD; ++r) w[r] = tw[r * k * TWS];
+        }
+        dft<R, INV, RAD, (S > 0)>(v[q], w);
+        const int base = (j - k) * RAD + k;
+        if constexpr (LAST) {
+#pragma unroll
+          for (int r = 0; r < RAD; ++r) st(l, base + r * NS, v[q][r]);
+        } else {
+#pragma unroll
+          for (int r = 0; r < RAD; ++r) xb[MAP::template idx<S>(base + r * NS, l)] = v[q][r];
+        }
+      }
+    }
+    if constexpr (!LAST) {
+      __syncthreads();
+      RegStage<R, L, INV, NT, NLINES, MAP, S + 1, NS * RAD>::run(xb, tw, ld, st);
+    }
+  }
+};
+
+// Transform NLINES lines.  All NT threads must call it; the exchange buffer
+// xb (MAP::elems() elements) must not be in use by any thread.  Returns with
+// no synchronisation after the last stage.
+template <typename R, int L, bool INV, int NT, int NLINES, class MAP = MapInterleaved<R, L, NLINES>, class LD,
+          class ST>
+__device__ __forceinline__ void fft_lines(C2<R>* xb, const C2<R>* __restrict__ tw, const LD& ld, const ST& st) {
+  static_assert(rstages<R>(L) > 0, "unsupported FFT length");
+  RegStage<R, L, INV, NT, NLINES, MAP, 0, 1>::run(xb, tw, ld, st);
+}
+
+// Generic strided pass: NLINES consecutive lines lam = outer * hz + z of one
+// field per CTA (blockIdx.x = f + nfields * tile), so no z tile is partly
+// empty.  Op supplies load(f, outer, z, p), out_index(p) (-1: dropped) and
+// store(f, outer, z, i, v).
+template <typename R, int L, bool INV, int NLINES, int NT, class Op>
+__global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op op, const C2<R>* __restrict__ tw, int nlines) {
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
+  const int f = blockIdx.x % op.nfields;
+  const int tile = blockIdx.x / op.nfields;
+  const int lam = tile * NLINES + (int)(threadIdx.x % NLINES);
+  const bool ok = lam < nlines;
+  const int outer = ok ? lam / op.hz : 0;
+  const int z = ok ? lam - outer * op.hz : 0;
+  static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
+  fft_lines<R, L, INV, NT, NLINES>(
+      xb, tw, [&](int, int p) { return ok ? op.load(f, outer, z, p) : czero<R>(); },
+      [&](int, int p, C2<R> v) {
+        const int i = op.out_index(p);
+        if (ok && i >= 0) op.store(f, outer, z, i, v);
+      });
+}
+
+// ---------------------------------------------------------------------------
+// P5: x-forward of the three cross-product fields, keep N of M modes, scale
+// N^3/M^3 (dealiased.rs:102-109), Leray projection (spectral_ops.rs:114-151)
+// and the stage epilogue.  A CTA takes NLINES consecutive (iy, z) lines; the
+// fields are transformed one after another into shared memory (kept modes
+// only), then the epilogue runs over the CTA's N x NLINES modes with
+// consecutive lanes on consecutive z.
+// ---------------------------------------------------------------------------
+template <typename R> struct P5Args {
+  int N, M, H, nlines;
+  R s_out, ks;
+  const C2<R>* in; size_t fsin;   // (M, N, H)
+  StageArgs<R> st;
+};
+
+template <typename R> struct P5Lines { static constexpr int value = sizeof(R) == 8 ? 4 : 8; };
+
+template <typename R, int L, int NLINES, int NT>
+__global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT, true>())
+k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
+  constexpr int N = 2 * L / 3;
+  static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
+  C2<R>* keep = xb + rsmem_elems<R, L, NLINES>();   // 3 fields x N x NLINES
+  const int H = a.H;
+  {
+    const int lam = blockIdx.x * NLINES + (int)(threadIdx.x % NLINES);
+    const bool ok = lam < a.nlines;
+    const int iy = ok ? lam / H : 0;
+    const int z = ok ? lam - iy * H : 0;
+    sfor<3>([&](auto cc) {
+      constexpr int C = decltype(cc)::value;
+      if (C > 0) __syncthreads();   // xb is reused
+      const C2<R>* src = a.in + (size_t)C * a.fsin + (size_t)iy * H + z;
+      fft_lines<R, L, false, NT, NLINES>(
+          xb, tw, [&](int, int p) { return ok ? src[(size_t)p * N * H] : czero<R>(); },
+          [&](int, int p, C2<R> v) {
+            const int ix = unpad_pos(p, N, L);
+            if (ix >= 0) keep[(C * N + ix) * NLINES + (int)(threadIdx.x % NLINES)] = v;
+          });
+    });
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int e = threadIdx.x; e < N * NLINES; e += NT) {
+    const int ix = e / NLINES, l = e % NLINES;
+    const int lam = blockIdx.x * NLINES + l;
+    if (lam >= a.nlines) continue;
+    const int iy = lam / H;
+    const int z = lam - iy * H;
+    const int kxi = signed_k(ix, N), kyi = signed_k(iy, N);
+    const R kx = a.ks * (R)kxi, ky = a.ks * (R)kyi, kz = a.ks * (R)z;
+    C2<R> nl[3] = {cscale<R>(keep[e], a.s_out), cscale<R>(keep[N * NLINES + e], a.s_out),
+                   cscale<R>(keep[2 * N * NLINES + e], a.s_out)};
+    const R k2 = (kx * kx + ky * ky) + kz * kz;
+    if (!(k2 < R(1e-30))) {
+      const R inv = R(1) / k2;
+      const C2<R> kd = cmk<R>((kx * nl[0].x + ky * nl[1].x) + kz * nl[2].x,
+                              (kx * nl[0].y + ky * nl[1].y) + kz * nl[2].y);
+      nl[0] = cmk<R>(nl[0].x - kx * kd.x * inv, nl[0].y - kx * kd.y * inv);
+      nl[1] = cmk<R>(nl[1].x - ky * kd.x * inv, nl[1].y - ky * kd.y * inv);
+      nl[2] = cmk<R>(nl[2].x - kz * kd.x * inv, nl[2].y - kz * kd.y * inv);
+    }
+    const int m = kxi * kxi + kyi * kyi + z * z;
+    stage_apply<R>(a.st, ((size_t)ix * N + iy) * H + z, m, k2, nl);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// P3 on the register engine: per CTA CP column pairs.  Inverse lines (6 CP):
+// l = t * 2CP + c, the packed pair t of column c ((u_x, u_y), (u_z, w_x),
+// (w_y, w_z)); the first stage packs straight from global memory with the
+// Hermitian extension (z-line helpers above), the last stage writes the
+// physical values to buffer B.  The cross product then writes the forward
+// lines (3 CP) to buffer A: l = t * CP + pr with (c_x^A + i c_y^A),
+// (c_z^A + i c_z^B), (c_x^B + i c_y^B) for the columns A, B of pair pr.  The
+// forward transform reads A, exchanges through B and writes its spectra back
+// to A, from where the kept H modes are unpacked and stored.
+// ---------------------------------------------------------------------------
+template <typename R, int M, int CP>
+__host__ __device__ constexpr int p3_threads() {
+  return cmin(rthreads<R, M, 6 * CP>(), 384);
+}
+
+template <typename R, int M, int CP, int NT>
+__global__ void __launch_bounds__(NT, M >= 768 ? 1 : cmax(1, (sizeof(R) == 8 ? 768 : 512) / NT))
+k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
+  constexpr int N = 2 * M / 3;
+  constexpr int H = N / 2 + 1;
+  constexpr int LP = zpad_len<R>(M);
+  constexpr int NI = 6 * CP, NF = 3 * CP;
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  C2<R>* A = reinterpret_cast<C2<R>*>(vk_smem);
+  C2<R>* B = A + NI * LP;
+  const int col0 = blockIdx.x * 2 * CP;
+  fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>>(
+      A, tw,
+      [&](int l, int p) -> C2<R> {
+        const int t = l / (2 * CP);
+        const int col = col0 + l % (2 * CP);
+        if (col >= a.ncols) return czero<R>();
+        const bool lo = p < H;
+        if (!lo && p <= M - H) return czero<R>();
+        const int k = lo ? p : M - p;
+        const C2<R>* src = a.in + (size_t)col * H + k;
+        const C2<R> X = src[(size_t)(2 * t) * a.fsin];
+        const C2<R> Y = src[(size_t)(2 * t + 1) * a.fsin];
+        if (p == 0) return cmk<R>(X.x, Y.x);
+        return lo ? cmk<R>(X.x - Y.y, X.y + Y.x) : cmk<R>(X.x + Y.y, Y.x - X.y);
+      },
+      [&](int l, int p, C2<R> v) { B[l * LP + zi<R>(p)] = v; });
+  __syncthreads();
+  for (int e = threadIdx.x; e < CP * M; e += NT) {
+    const int pr = e / M, p = e % M;
+    const int zp = zi<R>(p);
+    R c[2][3];
+#pragma unroll
+    for (int cc = 0; cc < 2; ++cc) {
+      const int col = 2 * pr + cc;
+      const C2<R> z1 = B[col * LP + zp], z2 = B[(2 * CP + col) * LP + zp], z3 = B[(4 * CP + col) * LP + zp];
+      const R ux = z1.x, uy = z1.y, uz = z2.x, wx = z2.y, wy = z3.x, wz = z3.y;
+      c[cc][0] = uy * wz - uz * wy;
+      c[cc][1] = uz * wx - ux * wz;
+      c[cc][2] = ux * wy - uy * wx;
+    }
+    A[pr * LP + zp] = cmk<R>(c[0][0], c[0][1]);
+    A[(CP + pr) * LP + zp] = cmk<R>(c[0][2], c[1][2]);
+    A[(2 * CP + pr) * LP + zp] = cmk<R>(c[1][0], c[1][1]);
+  }
+  __syncthreads();
+  fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>>(
+      B, tw, [&](int l, int p) { return A[l * LP + zi<R>(p)]; },
+      [&](int l, int p, C2<R> v) { A[l * LP + zi<R>(p)] = v; });
+  __syncthreads();
+  for (int e = threadIdx.x; e < CP * 3 * H; e += NT) {
+    const int k = e % H;
+    const int t = (e / H) % 3;
+    const int pr = e / (3 * H);
+    C2<R> X, Y;
+    zunpack<R>(A + (t * CP + pr) * LP, M, k, X, Y);
+    const int ca = col0 + 2 * pr, cb = ca + 1;
+    if (t == 0) {
+      if (ca < a.ncols) {
+        a.out[(size_t)ca * H + k] = X;
+        a.out[a.fsout + (size_t)ca * H + k] = Y;
+      }
+    } else if (t == 1) {
+      if (ca < a.ncols) a.out[2 * a.fsout + (size_t)ca * H + k] = X;
+      if (cb < a.ncols) a.out[2 * a.fsout + (size_t)cb * H + k] = Y;
+    } else {
+      if (cb < a.ncols) {
+        a.out[(size_t)cb * H + k] = X;
+        a.out[a.fsout + (size_t)cb * H + k] = Y;
+      }
+    }
+  }
+}
+
+}  // namespace vk

@@ -1,0 +1,165 @@
+"""Run loop and the long workloads of the periodic step.
+
+``run_to_time`` is the time loop of vonkarman-bin (run.rs:107-182: step, then
+Tier-1 diagnostics, stop at the first step whose time reaches ``max_time``)
+with the diagnostics recorded on the device by ``vk_run`` and read back once
+per chunk instead of once per step.
+
+Two workloads are run from here (``python -m vonkarman_gb300.runs <name>``):
+
+* ``tubes``  -- anti-parallel Lamb-Oseen tubes (circulation +-1, core radius
+  0.25, separation 1.0 about (pi, pi), centre lines displaced in x by
+  0.1 sin z), nu = 5e-4, adaptive CFL 0.5, to t = 5, Tier-1 after every step,
+  FP32-bulk against FP64: steps/s of both forms and the relative error of the
+  energy, enstrophy and max|omega| at t = 5.
+* ``ascent`` -- random isotropic start (kp = 3, E = 0.5), nu = 2e-3, fixed
+  dt = 1e-3, 1000 steps, 20 level-1 checkpoints: the FP32-bulk and FP64
+  gradients of the final enstrophy, the adjoint/forward cost ratio of both
+  forms, the FP32-bulk gradient error against the FP64 one, and 10
+  projected-gradient ascent iterations on the sphere <u, u> = 1.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import time
+
+import numpy as np
+
+from . import ics, optimize
+from .solver import GridSpec, Periodic3D, SolverOptions, l2_inner
+
+
+def run_to_time(solver: Periodic3D, t_end: float, every: int = 1, max_chunk: int = 200):
+    """Step until ``solver.time() >= t_end`` (the stop rule of run.rs:152-155)
+    and return the Tier-1 records of every ``every``-th step.  Chunks are sized
+    from the current dt so that the loop does not pass the first step that
+    reaches ``t_end``; the last few steps are taken one at a time."""
+    recs = []
+    while solver.time() < t_end:
+        dt = solver.dt()
+        left = t_end - solver.time()
+        k = int(0.9 * left / dt) if dt > 0 else 1
+        k = max(1, min(max_chunk, k))
+        if every > 1:
+            k = max(every, k - k % every)
+        recs.extend(solver.run(k, every))
+    return recs
+
+
+def interp_at(recs, t: float, name: str) -> float:
+    """Linear interpolation of a Tier-1 field at time t between the records
+    that bracket it."""
+    ts = np.array([r.time for r in recs])
+    vs = np.array([getattr(r, name) for r in recs])
+    return float(np.interp(t, ts, vs))
+
+
+def _timed_rate(solver: Periodic3D, steps: int) -> float:
+    solver.step(3)
+    ms = solver.step_timed(steps)
+    return 1000.0 * steps / ms
+
+
+def tubes(n: int = 512, nu: float = 5e-4, t_end: float = 5.0, rate_steps: int = 20, device: int = 0) -> dict:
+    grid = GridSpec(n)
+    u0 = ics.lamb_oseen_tubes(n, circulation=1.0, sigma=0.25, separation=1.0, eps=0.1)
+    out = {"workload": f"anti-parallel Lamb-Oseen tubes N={n}, nu={nu}, adaptive CFL 0.5, to t={t_end}, "
+                       "Tier-1 after every step", "forms": {}}
+    series = {}
+    for prec in ("fp64", "fp32bulk"):
+        s = Periodic3D(grid, nu, u0, SolverOptions(precision=prec, device=device))
+        t0 = time.perf_counter()
+        recs = run_to_time(s, t_end)
+        wall = time.perf_counter() - t0
+        series[prec] = recs
+        u_end = s.u_hat() if prec == "fp64" else None
+        rate = _timed_rate(s, rate_steps)
+        out["forms"][prec] = {"steps": len(recs), "t_last": recs[-1].time, "wall_s": wall,
+                              "steps_per_s_with_tier1": len(recs) / wall,
+                              "steps_per_s": rate,
+                              "energy_t_end": interp_at(recs, t_end, "energy"),
+                              "enstrophy_t_end": interp_at(recs, t_end, "enstrophy"),
+                              "max_vorticity_t_end": interp_at(recs, t_end, "max_vorticity")}
+        s.close()
+        del u_end
+    f64, f32 = out["forms"]["fp64"], out["forms"]["fp32bulk"]
+    out["speedup_fp32bulk_over_fp64"] = f32["steps_per_s"] / f64["steps_per_s"]
+    out["rel_error_at_t_end"] = {k: abs(f32[k + "_t_end"] - f64[k + "_t_end"]) / abs(f64[k + "_t_end"])
+                                 for k in ("energy", "enstrophy", "max_vorticity")}
+    # the largest relative deviation over the run, at equal times
+    a, b = series["fp64"], series["fp32bulk"]
+    tt = np.array([r.time for r in a])
+    tt = tt[tt <= min(a[-1].time, b[-1].time)]
+    worst = {}
+    for k in ("energy", "enstrophy", "max_vorticity"):
+        va = np.interp(tt, [r.time for r in a], [getattr(r, k) for r in a])
+        vb = np.interp(tt, [r.time for r in b], [getattr(r, k) for r in b])
+        worst[k] = float(np.max(np.abs(vb - va) / np.abs(va)))
+    out["max_rel_deviation_over_run"] = worst
+    return out
+
+
+def _grad_rel(g, g_ref, n: int) -> float:
+    d = [a - b for a, b in zip(g, g_ref)]
+    return math.sqrt(l2_inner(d, d, n) / l2_inner(g_ref, g_ref, n))
+
+
+def ascent(n: int = 256, nu: float = 2e-3, dt: float = 1e-3, nsteps: int = 1000, nsnap: int = 20,
+           iters: int = 10, device: int = 0) -> dict:
+    grid = GridSpec(n)
+    u0 = ics.project_control(ics.von_karman_isotropic(n, kp=3.0, energy=0.5, seed=42), n)
+    r = math.sqrt(l2_inner(u0, u0, n))
+    u0 = [c / r for c in u0]          # on the sphere <u, u> = 1 (E = 0.5)
+    out = {"workload": f"random isotropic kp=3 E=0.5, N={n}, nu={nu}, fixed dt={dt}, {nsteps} steps, "
+                       f"{nsnap} level-1 checkpoints", "forms": {}}
+    grads = {}
+    for prec in ("fp64", "fp32bulk"):
+        s = Periodic3D(grid, nu, u0, SolverOptions(precision=prec, dt_mode="fixed", dt_fixed=dt, device=device))
+        s.step(2)
+        s.restore_state(u0, 0.0, 0, dt)
+        s.event_mark(0)
+        s.step(nsteps)
+        s.event_mark(1)
+        s.restore_state(u0, 0.0, 0, dt)
+        s.event_mark(2)
+        J = s.adjoint_forward(nsteps, nsnap)
+        s.event_mark(3)
+        grads[prec] = s.adjoint_backward()
+        s.event_mark(4)
+        fwd, af, ab = s.event_elapsed(0, 1), s.event_elapsed(2, 3), s.event_elapsed(3, 4)
+        out["forms"][prec] = {"J": J, "forward_ms": fwd, "adjoint_forward_ms": af, "adjoint_backward_ms": ab,
+                              "total_over_forward": (af + ab) / fwd,
+                              "gradient_norm": math.sqrt(l2_inner(grads[prec], grads[prec], n))}
+        s.close()
+    out["fp32bulk_vs_fp64_gradient_rel_l2"] = _grad_rel(grads["fp32bulk"], grads["fp64"], n)
+    out["fp32bulk_vs_fp64_J_rel"] = abs(out["forms"]["fp32bulk"]["J"] - out["forms"]["fp64"]["J"]) / abs(
+        out["forms"]["fp64"]["J"])
+    del grads
+    t0 = time.perf_counter()
+    res = optimize.enstrophy_ascent(grid, nu, dt, u0, nsteps, iters=iters, nsnap=nsnap, precision="fp32bulk")
+    out["ascent"] = {"iterations": iters, "J": res.J, "grad_norm": res.grad_norm,
+                     "energy_final": 0.5 * l2_inner(res.u, res.u, n), "wall_s": time.perf_counter() - t0}
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("workload", choices=["tubes", "ascent"])
+    ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--t-end", type=float, default=5.0)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--iters", type=int, default=10)
+    ap.add_argument("--device", type=int, default=0)
+    a = ap.parse_args(argv)
+    if a.workload == "tubes":
+        r = tubes(n=a.n or 512, t_end=a.t_end, device=a.device)
+    else:
+        r = ascent(n=a.n or 256, nsteps=a.steps, iters=a.iters, device=a.device)
+    print(json.dumps(r))
+
+
+if __name__ == "__main__":
+    main()

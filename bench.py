@@ -491,7 +491,8 @@ def run_ours(args, d: Dist):
                      "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
         "fp64_roofline": {"kernel": dom, "achieved": dom_gflops, "peak": fp64_peak, "unit": "GFLOP/s",
                           "frac": dom_gflops / fp64_peak, "peak_source": "measured live (FP64 FMA probe)",
-                          "note": "the FP64 form is bound by GB300's FP64 pipe, not HBM"},
+                          "note": "the FP64 form is bound by GB300's FP64 pipe, not HBM"}
+        if args.precision == "fp64" else None,
         "passes": passes,
         "cpu_baseline": cpu,
         "e2e": e2e,

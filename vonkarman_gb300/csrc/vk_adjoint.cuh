@@ -22,6 +22,8 @@
 namespace vk {
 
 // A1: fields 0..4 as P1 on x; fields 5..7 = Pad(mul * S_out * P nbar / w_M).
+// Kinds: 0 = u_c, 1 = i kx u, 2 = c_bar (Leray projection and ETD factor
+// applied at the load, three loads per position).
 template <typename R> struct OpAdjXInv {
   int nfields, hz;
   int N, M;
@@ -30,39 +32,52 @@ template <typename R> struct OpAdjXInv {
   const C2<R>* nb;                     // cotangent source (3 components, stride cs)
   const double* etd; int slot; double fac; const double* dt;   // mul = fac dt etd[slot] if slot >= 0
   C2<R>* out; size_t fs;
-  __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
+  static constexpr bool STAGED_ANY = false;
+  template <int K> __host__ __device__ static constexpr bool staged() { return false; }
+  static constexpr int NKIND = 3;
+  __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : f < 5 ? 1 : 2; }
+  template <int K> __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
     const int ix = unpad_pos(p, N, M);
-    if (ix < 0) return czero<R>();
-    const size_t idx = ((size_t)ix * N + iy) * hz + z;
-    const int kxi = signed_k(ix, N), kyi = signed_k(iy, N);
-    if (f < 5) {
-      const int c = f < 3 ? f : f - 2;
-      C2<R> v = cscale<R>(in[(size_t)c * cs + idx], s_in);
-      if (f >= 3) {
-        const R kx = ks * (R)kxi;
+    if constexpr (K < 2) {
+      const int c = K == 0 ? f : f - 2;
+      return ix < 0 ? czero<R>() : in[(size_t)c * cs + ((size_t)ix * N + iy) * hz + z];
+    } else {
+      if (ix < 0) return czero<R>();
+      const size_t idx = ((size_t)ix * N + iy) * hz + z;
+      const int kxi = signed_k(ix, N), kyi = signed_k(iy, N);
+      const int c = f - 5;
+      C2<R> b[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) b[j] = nb[(size_t)j * cs + idx];
+      const R kx = ks * (R)kxi, ky = ks * (R)kyi, kz = ks * (R)z;
+      const R k2 = (kx * kx + ky * ky) + kz * kz;
+      C2<R> v = b[c];
+      if (!(k2 < R(1e-30))) {
+        const R inv = R(1) / k2;
+        const C2<R> kd = cmk<R>((kx * b[0].x + ky * b[1].x) + kz * b[2].x, (kx * b[0].y + ky * b[1].y) + kz * b[2].y);
+        const R kc = c == 0 ? kx : c == 1 ? ky : kz;
+        v = cmk<R>(v.x - kc * kd.x * inv, v.y - kc * kd.y * inv);
+      }
+      R mul = s_cbar * (z == 0 ? R(1) : R(0.5));
+      if (slot >= 0) {
+        const int m = kxi * kxi + kyi * kyi + z * z;
+        mul *= (R)(fac * (*dt) * etd[(size_t)m * ETD_STRIDE + slot]);
+      }
+      return cscale<R>(v, mul);
+    }
+  }
+  template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int p, C2<R> v) const {
+    if constexpr (K == 2) {
+      return v;
+    } else {
+      v = cscale<R>(v, s_in);
+      if constexpr (K == 1) {
+        const int ix = unpad_pos(p, N, M);
+        const R kx = ks * (R)signed_k(ix < 0 ? 0 : ix, N);
         v = cmk<R>(-kx * v.y, kx * v.x);
       }
       return v;
     }
-    const int c = f - 5;
-    C2<R> b[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) b[j] = nb[(size_t)j * cs + idx];
-    const R kx = ks * (R)kxi, ky = ks * (R)kyi, kz = ks * (R)z;
-    const R k2 = (kx * kx + ky * ky) + kz * kz;
-    C2<R> v = b[c];
-    if (!(k2 < R(1e-30))) {
-      const R inv = R(1) / k2;
-      const C2<R> kd = cmk<R>((kx * b[0].x + ky * b[1].x) + kz * b[2].x, (kx * b[0].y + ky * b[1].y) + kz * b[2].y);
-      const R kc = c == 0 ? kx : c == 1 ? ky : kz;
-      v = cmk<R>(v.x - kc * kd.x * inv, v.y - kc * kd.y * inv);
-    }
-    R mul = s_cbar * (z == 0 ? R(1) : R(0.5));
-    if (slot >= 0) {
-      const int m = kxi * kxi + kyi * kyi + z * z;
-      mul *= (R)(fac * (*dt) * etd[(size_t)m * ETD_STRIDE + slot]);
-    }
-    return cscale<R>(v, mul);
   }
   __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int iy, int z, int i, C2<R> v) const {
@@ -71,14 +86,31 @@ template <typename R> struct OpAdjXInv {
 };
 
 // A2: fields 0..5 as P2 (u, omega), fields 6..8 = y-inverse of c_bar.
+// Kinds as P2, then one more for c_bar.
 template <typename R> struct OpAdjYInv {
   OpYInv<R> base;   // reads input fields 0..4
   int nfields, hz;
-  __device__ __forceinline__ C2<R> load(int f, int x, int z, int p) const {
-    if (f < 6) return base.load(f, x, z, p);
-    const int iy = unpad_pos(p, base.N, base.M);
-    if (iy < 0) return czero<R>();
-    return base.in[(size_t)(f - 1) * base.fsin + ((size_t)x * base.N + iy) * hz + z];
+  static constexpr bool STAGED_ANY = OpYInv<R>::STAGED_ANY;
+  static constexpr int KC = OpYInv<R>::NKIND;   // the c_bar kind
+  template <int K> __host__ __device__ static constexpr bool staged() {
+    return K < KC && OpYInv<R>::template staged<K>();
+  }
+  static constexpr int NKIND = KC + 1;
+  __host__ __device__ __forceinline__ int kind(int f) const { return f < 6 ? base.kind(f) : KC; }
+  template <int K> __device__ __forceinline__ auto load(int f, int x, int z, int p) const {
+    if constexpr (K < KC) {
+      return base.template load<K>(f, x, z, p);
+    } else {
+      const int iy = unpad_pos(p, base.N, base.M);
+      return iy < 0 ? czero<R>() : base.in[(size_t)(f - 1) * base.fsin + ((size_t)x * base.N + iy) * hz + z];
+    }
+  }
+  template <int K, class T> __device__ __forceinline__ C2<R> prep(int f, int x, int z, int p, const T& r) const {
+    if constexpr (K < KC) {
+      return base.template prep<K>(f, x, z, p, r);
+    } else {
+      return r;
+    }
   }
   __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
@@ -200,6 +232,8 @@ __global__ void __launch_bounds__(NT, min_blocks<NT>()) k_adj_z(A3Args<R> a, con
 //   ADJ_A  (x = a): acc += E2 y; n1b += dt a21 y
 //   ADJ_U  (x = u): ub = acc + y
 // (ub = cotangent of the step's output, E = exp(z), E2 = exp(z/2)).
+// Inputs of all three components are loaded before any store (see
+// stage_apply).
 template <typename R>
 __device__ __forceinline__ void adj_stage_apply(const AdjStageArgs<R>& s, size_t idx, int m, const C2<R>* y) {
   const size_t cs = s.cs;
@@ -210,43 +244,66 @@ __device__ __forceinline__ void adj_stage_apply(const AdjStageArgs<R>& s, size_t
   }
   const double dt = *s.dt;
   const double* e = s.etd + (size_t)m * ETD_STRIDE;
+  switch (s.op) {
+    case ADJ_C: {
+      const R E = (R)e[E_FULL];
+      const R nb_u = (R)(dt * e[E_B23]), nb_y = (R)(2.0 * dt * e[E_A41]);
+      const R n1_u = (R)(dt * e[E_B1]), n1_y = (R)(-dt * e[E_A41]);
+      C2<R> ub[3];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const size_t i = c * cs + idx;
-    const C2<R> yy = y[c];
-    switch (s.op) {
-      case ADJ_C: {
-        const C2<R> ub = s.ub[i];
-        const R E = (R)e[E_FULL];
-        s.acc[i] = cmk<R>(E * (ub.x + yy.x), E * (ub.y + yy.y));
-        s.nb[i] = axpby<R>((R)(dt * e[E_B23]), ub, (R)(2.0 * dt * e[E_A41]), yy);
-        s.n1b[i] = axpby<R>((R)(dt * e[E_B1]), ub, (R)(-dt * e[E_A41]), yy);
-        break;
+      for (int c = 0; c < 3; ++c) ub[c] = s.ub[c * cs + idx];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const size_t i = c * cs + idx;
+        s.acc[i] = cmk<R>(E * (ub[c].x + y[c].x), E * (ub[c].y + y[c].y));
+        s.nb[i] = axpby<R>(nb_u, ub[c], nb_y, y[c]);
+        s.n1b[i] = axpby<R>(n1_u, ub[c], n1_y, y[c]);
       }
-      case ADJ_B: {
-        const C2<R> ub = s.ub[i];
-        const C2<R> ac = s.acc[i];
-        const R E2 = (R)e[E_HALF];
-        s.acc[i] = cmk<R>(ac.x + E2 * yy.x, ac.y + E2 * yy.y);
-        s.nb[i] = axpby<R>((R)(dt * e[E_B23]), ub, (R)(dt * e[E_A21]), yy);
-        break;
-      }
-      case ADJ_A: {
-        const C2<R> ac = s.acc[i];
-        const C2<R> n1 = s.n1b[i];
-        const R E2 = (R)e[E_HALF];
-        const R q = (R)(dt * e[E_A21]);
-        s.acc[i] = cmk<R>(ac.x + E2 * yy.x, ac.y + E2 * yy.y);
-        s.n1b[i] = cmk<R>(n1.x + q * yy.x, n1.y + q * yy.y);
-        break;
-      }
-      case ADJ_U: {
-        const C2<R> ac = s.acc[i];
-        s.ub[i] = cmk<R>(ac.x + yy.x, ac.y + yy.y);
-        break;
-      }
-      default: break;
+      break;
     }
+    case ADJ_B: {
+      const R E2 = (R)e[E_HALF];
+      const R nb_u = (R)(dt * e[E_B23]), nb_y = (R)(dt * e[E_A21]);
+      C2<R> ub[3], ac[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        ub[c] = s.ub[c * cs + idx];
+        ac[c] = s.acc[c * cs + idx];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const size_t i = c * cs + idx;
+        s.acc[i] = cmk<R>(ac[c].x + E2 * y[c].x, ac[c].y + E2 * y[c].y);
+        s.nb[i] = axpby<R>(nb_u, ub[c], nb_y, y[c]);
+      }
+      break;
+    }
+    case ADJ_A: {
+      const R E2 = (R)e[E_HALF];
+      const R q = (R)(dt * e[E_A21]);
+      C2<R> ac[3], n1[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        ac[c] = s.acc[c * cs + idx];
+        n1[c] = s.n1b[c * cs + idx];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const size_t i = c * cs + idx;
+        s.acc[i] = cmk<R>(ac[c].x + E2 * y[c].x, ac[c].y + E2 * y[c].y);
+        s.n1b[i] = cmk<R>(n1[c].x + q * y[c].x, n1[c].y + q * y[c].y);
+      }
+      break;
+    }
+    case ADJ_U: {
+      C2<R> ac[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) ac[c] = s.acc[c * cs + idx];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) s.ub[c * cs + idx] = cmk<R>(ac[c].x + y[c].x, ac[c].y + y[c].y);
+      break;
+    }
+    default: break;
   }
 }
 
@@ -291,7 +348,7 @@ k_adj_p5(A5Args<R> a, const C2<R>* __restrict__ tw) {
       if (C > 0) __syncthreads();   // xb is reused
       const C2<R>* src = a.in + (size_t)C * a.fsin + (size_t)iy * H + z;
       fft_lines<R, L, false, NT, NLINES>(
-          xb, tw, [&](int, int p) { return ok ? src[(size_t)p * N * H] : czero<R>(); },
+          xb, tw, [&](int, int p) { return src[(size_t)p * N * H]; }, PrepNone{},
           [&](int, int p, C2<R> v) {
             const int ix = unpad_pos(p, N, L);
             if (ix < 0) return;

@@ -32,18 +32,23 @@ inline cudaError_t prepare_kernel(size_t smem) {
 
 // Register-resident strided pass (k_lines): nouter * hz lines per field in
 // tiles of NLINES.
-template <typename R> struct NLof { static constexpr int value = 8; };
-template <typename R, int L> __host__ __device__ constexpr int lines_nt() {
-  return cmin(rthreads<R, L, NLof<R>::value>(), 384);
-}
+// Lines per CTA: 8 (row segments of 64 bytes in FP32, 128 in FP64).  X passes
+// (FFT axis = slowest array dimension) are marked so that the tile can differ
+// from the y passes; 16-line FP32 x tiles measured no faster.
+template <typename R, int L, bool XAXIS> struct NLof {
+  static constexpr int value = 8;
+};
 
-template <typename R, int L, bool INV, class Op>
+template <typename R, int L, bool INV, bool XAXIS = false, class Op>
 inline cudaError_t launch_lines(const Op& op, int nouter, const C2<R>* tw, cudaStream_t s) {
-  constexpr int NLINES = NLof<R>::value;
-  constexpr int NT = lines_nt<R, L>();
-  const size_t smem = (size_t)rsmem_elems<R, L, NLINES>() * sizeof(C2<R>);
+  constexpr int NLINES = NLof<R, L, XAXIS>::value;
+  constexpr int NT = cmin(rthreads<R, L, NLINES>(), 384);
+  const size_t smem = lines_smem_bytes<R, L, NLINES>(op);
   constexpr auto kern = k_lines<R, L, INV, NLINES, NT, Op>;
-  cudaError_t e = prepare_kernel<kern>(smem);
+  // the attribute is sized for the staging tile, so that launches of the
+  // same kernel without it do not need a second setting
+  cudaError_t e = prepare_kernel<kern>((size_t)(rsmem_elems<R, L, NLINES>() + (Op::STAGED_ANY ? L * NLINES : 0)) *
+                                       sizeof(C2<R>));
   if (e != cudaSuccess) return e;
   const int nlines = nouter * op.hz;
   const int ntiles = (nlines + NLINES - 1) / NLINES;
@@ -66,7 +71,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   {
     TimerScope ts(p.timer, PASS_P1, s);
     OpXInv<R> o{5, H, N, M, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fsA1};
-    e = launch_lines<R, M, true>(o, N, p.twM, s);
+    e = launch_lines<R, M, true, true>(o, N, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   // P2
@@ -132,7 +137,7 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
     TimerScope ts(p.timer, PASS_A1, s);
     OpAdjXInv<R> o{8, H, N, M, (R)(1.0 / ((double)N * N * N)), (R)(1.0 / scale), ks,
                    p.x, p.cs, p.nb, p.etd, p.slot, p.fac, p.dt, p.bufA, fsA1};
-    e = launch_lines<R, M, true>(o, N, p.twM, s);
+    e = launch_lines<R, M, true, true>(o, N, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   {
@@ -190,7 +195,7 @@ inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
     TimerScope ts(p.timer, PASS_NX, s);
     const int nf = need_w ? 5 : 3;
     OpXInv<R> o{nf, H, N, N, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fs};
-    e = launch_lines<R, N, true>(o, N, p.twN, s);
+    e = launch_lines<R, N, true, true>(o, N, p.twN, s);
     if (e != cudaSuccess) return e;
   }
   {
@@ -253,8 +258,8 @@ inline cudaError_t fxy_pass(const FftParams<R>& p, bool inverse, cudaStream_t s)
   OpPlainC2C<R, AXIS> o{1, hz, p.nx, p.ny, p.cplx};
   const int nouter = AXIS == 0 ? p.ny : p.nx;
   const C2<R>* tw = AXIS == 0 ? p.twx : p.twy;
-  if (inverse) return launch_lines<R, L, true>(o, nouter, tw, s);
-  return launch_lines<R, L, false>(o, nouter, tw, s);
+  if (inverse) return launch_lines<R, L, true, AXIS == 0>(o, nouter, tw, s);
+  return launch_lines<R, L, false, AXIS == 0>(o, nouter, tw, s);
 }
 
 #define VK_FOR_LENGTHS(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(12) X(24) X(48) X(96) X(192) X(384) X(768)

@@ -47,6 +47,8 @@ __device__ __forceinline__ C2<R> cmulc(C2<R> a, C2<R> b) {
 }
 template <typename R>
 __device__ __forceinline__ C2<R> czero() { return cmk<R>(R(0), R(0)); }
+// two loaded complex values (raw inputs that a later step combines)
+template <typename R> struct C2x2 { C2<R> a, b; };
 
 // ---------------------------------------------------------------------------
 // Radix plans.  The first stage carries no twiddles, so the largest radix goes

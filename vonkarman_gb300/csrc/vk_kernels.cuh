@@ -54,21 +54,27 @@ template <int NT> __host__ __device__ constexpr int min_blocks() { return cmax(1
 // P1 / N-grid X: x-inverse of the spectral state, zero-pad N -> M (M == N on
 // the N grid).  Fields: 0..2 = u_c, 3 = i kx u_y, 4 = i kx u_z.  s_in folds the
 // 1/M^3 of the padded c2r and the (M/N)^3 pre-scale (dealiased.rs:43,:45-62)
-// into one factor 1/N^3.
+// into one factor 1/N^3.  Kinds: 0 = u_c, 1 = i kx u.
 template <typename R> struct OpXInv {
   int nfields, hz;
   int N, M;
   R s_in, ks;
   const C2<R>* in; size_t cs;
   C2<R>* out; size_t fs;
-  __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
+  static constexpr bool STAGED_ANY = false;
+  template <int K> __host__ __device__ static constexpr bool staged() { return false; }
+  static constexpr int NKIND = 2;
+  __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : 1; }
+  template <int K> __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
     const int ix = unpad_pos(p, N, M);
-    if (ix < 0) return czero<R>();
-    const int c = f < 3 ? f : f - 2;
-    C2<R> v = in[(size_t)c * cs + ((size_t)ix * N + iy) * hz + z];
+    const int c = K == 0 ? f : f - 2;
+    return ix < 0 ? czero<R>() : in[(size_t)c * cs + ((size_t)ix * N + iy) * hz + z];
+  }
+  template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int p, C2<R> v) const {
     v = cscale<R>(v, s_in);
-    if (f >= 3) {
-      const R kx = ks * (R)signed_k(ix, N);
+    if constexpr (K == 1) {
+      const int ix = unpad_pos(p, N, M);
+      const R kx = ks * (R)signed_k(ix < 0 ? 0 : ix, N);
       v = cmk<R>(-kx * v.y, kx * v.x);
     }
     return v;
@@ -82,33 +88,60 @@ template <typename R> struct OpXInv {
 // P2 / N-grid Y: y-inverse with zero-pad, forming u (g = 0..2) and
 // omega = i k x u (g = 3..5) from the x-transformed fields
 // (curl: vonkarman-core/src/spectral_ops.rs:81-108).  kx was applied in P1, ky
-// and kz are applied here (both are constant along an x line).
+// and kz are applied here (both are constant along an x line).  Kind 0 = u
+// (one load per position).  Omega needs two operand fields per position:
+// in FP32 one kind (1) stages them through shared memory; in FP64, whose
+// residency the staging tile would halve, kinds 1..3 (g = 3..5) combine them
+// at the load.
 template <typename R> struct OpYInv {
   int nfields, hz;
   int N, M, gbase;
   R ks;
   const C2<R>* in; size_t fsin;   // (M, N, H): Ux, Uy, Uz, Vy, Vz
   C2<R>* out; size_t fsout;       // (M, M, H)
-  __device__ __forceinline__ C2<R> load(int f, int x, int z, int p) const {
-    const int iy = unpad_pos(p, N, M);
-    if (iy < 0) return czero<R>();
+  static constexpr bool STAGED_ANY = sizeof(R) == 4;
+  template <int K> __host__ __device__ static constexpr bool staged() { return K == 1 && sizeof(R) == 4; }
+  static constexpr int NKIND = sizeof(R) == 4 ? 2 : 4;
+  __host__ __device__ __forceinline__ int kind(int f) const {
     const int g = f + gbase;
-    const size_t base = ((size_t)x * N + iy) * hz + z;
-    if (g < 3) return in[(size_t)g * fsin + base];
+    return g < 3 ? 0 : sizeof(R) == 4 ? 1 : g - 2;
+  }
+  // operands of omega_g: g = 3: (Uy, Uz); g = 4: (Ux, Vz); g = 5: (Ux, Vy)
+  __device__ __forceinline__ static int opa(int g) { return g == 3 ? 1 : 0; }
+  __device__ __forceinline__ static int opb(int g) { return g == 3 ? 2 : g == 4 ? 4 : 3; }
+  __device__ __forceinline__ C2<R> omega(int g, int z, int iy, const C2x2<R>& r) const {
     const R ky = ks * (R)signed_k(iy, N);
     const R kz = ks * (R)z;
-    if (g == 3) {  // i (ky Uz - kz Uy)
-      const C2<R> uy = in[fsin + base], uz = in[2 * fsin + base];
-      const C2<R> t = cmk<R>(ky * uz.x - kz * uy.x, ky * uz.y - kz * uy.y);
-      return cmul_i<R>(t);
+    if (g == 3) return cmul_i<R>(cmk<R>(ky * r.b.x - kz * r.a.x, ky * r.b.y - kz * r.a.y));  // i (ky Uz - kz Uy)
+    if (g == 4) return cmk<R>(-kz * r.a.y - r.b.x, kz * r.a.x - r.b.y);                     // i kz Ux - Vz
+    return cmk<R>(r.b.x + ky * r.a.y, r.b.y - ky * r.a.x);                                  // Vy - i ky Ux
+  }
+  template <int K> __device__ __forceinline__ auto load(int f, int x, int z, int p) const {
+    const int iy = unpad_pos(p, N, M);
+    const C2<R>* s = in + ((size_t)x * N + (iy < 0 ? 0 : iy)) * hz + z;
+    if constexpr (K == 0) {
+      return iy < 0 ? czero<R>() : s[(size_t)(f + gbase) * fsin];
+    } else if constexpr (sizeof(R) == 8) {
+      constexpr int g = K + 2;
+      if (iy < 0) return czero<R>();
+      C2x2<R> r;
+      r.a = s[(size_t)opa(g) * fsin];
+      r.b = s[(size_t)opb(g) * fsin];
+      return omega(g, z, iy, r);
+    } else {
+      const int g = f + gbase;
+      C2x2<R> r{};
+      if (iy >= 0) {
+        r.a = s[(size_t)opa(g) * fsin];
+        r.b = s[(size_t)opb(g) * fsin];
+      }
+      return r;
     }
-    if (g == 4) {  // i kz Ux - Vz
-      const C2<R> ux = in[base], vz = in[4 * fsin + base];
-      return cmk<R>(-kz * ux.y - vz.x, kz * ux.x - vz.y);
-    }
-    // g == 5: Vy - i ky Ux
-    const C2<R> ux = in[base], vy = in[3 * fsin + base];
-    return cmk<R>(vy.x + ky * ux.y, vy.y - ky * ux.x);
+  }
+  template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int, C2<R> v) const { return v; }
+  template <int K> __device__ __forceinline__ C2<R> prep(int f, int, int z, int p, const C2x2<R>& r) const {
+    const int iy = unpad_pos(p, N, M);
+    return omega(f + gbase, z, iy < 0 ? 0 : iy, r);
   }
   __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
@@ -123,9 +156,14 @@ template <typename R> struct OpYFwdTrunc {
   int N, M;
   const C2<R>* in; size_t fsin;   // (M, M, H)
   C2<R>* out; size_t fsout;       // (M, N, H)
-  __device__ __forceinline__ C2<R> load(int f, int x, int z, int p) const {
+  static constexpr bool STAGED_ANY = false;
+  template <int K> __host__ __device__ static constexpr bool staged() { return false; }
+  static constexpr int NKIND = 1;
+  __host__ __device__ __forceinline__ int kind(int) const { return 0; }
+  template <int K> __device__ __forceinline__ C2<R> load(int f, int x, int z, int p) const {
     return in[(size_t)f * fsin + ((size_t)x * M + p) * hz + z];
   }
+  template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int, C2<R> v) const { return v; }
   __device__ __forceinline__ int out_index(int p) const { return unpad_pos(p, N, M); }
   __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
     out[(size_t)f * fsout + ((size_t)x * N + i) * hz + z] = v;
@@ -138,10 +176,17 @@ template <typename R, int AXIS> struct OpPlainC2C {
   int nfields, hz;
   int nx, ny;
   C2<R>* data;
+  static constexpr bool STAGED_ANY = false;
+  template <int K> __host__ __device__ static constexpr bool staged() { return false; }
+  static constexpr int NKIND = 1;
+  __host__ __device__ __forceinline__ int kind(int) const { return 0; }
   __device__ __forceinline__ size_t at(int outer, int z, int p) const {
     return AXIS == 0 ? ((size_t)p * ny + outer) * hz + z : ((size_t)outer * ny + p) * hz + z;
   }
-  __device__ __forceinline__ C2<R> load(int, int outer, int z, int p) const { return data[at(outer, z, p)]; }
+  template <int K> __device__ __forceinline__ C2<R> load(int, int outer, int z, int p) const {
+    return data[at(outer, z, p)];
+  }
+  template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int, C2<R> v) const { return v; }
   __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int, int outer, int z, int i, C2<R> v) const { data[at(outer, z, i)] = v; }
 };
@@ -158,6 +203,9 @@ __device__ __forceinline__ C2<R> axpby(R a, C2<R> x, R b, C2<R> y) {
   return cmk<R>(a * x.x + b * y.x, a * x.y + b * y.y);
 }
 
+// The inputs of all three components are loaded before any result is
+// stored: a store may alias a later load as far as the compiler knows, so
+// interleaving them would serialise the loads.
 template <typename R>
 __device__ __forceinline__ void stage_apply(const StageArgs<R>& s, size_t idx, int m, R k2, const C2<R>* nl) {
   const size_t cs = s.cs;
@@ -167,92 +215,127 @@ __device__ __forceinline__ void stage_apply(const StageArgs<R>& s, size_t idx, i
     return;
   }
   const double dt = *s.dt;
+  C2<R> u[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) u[c] = s.u[c * cs + idx];
   if (s.op >= ST_RK4_1) {
     // rhs = N + (-nu k^2) state  (rk4.rs:30-45)
     const R visc = (R)(-s.nu) * k2;
-    const bool first = s.op == ST_RK4_1;
     const R half = (R)(0.5 * dt);
+    C2<R> st[3], a[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      st[c] = s.op == ST_RK4_1 ? u[c] : s.temp[c * cs + idx];
+      a[c] = s.op == ST_RK4_1 ? czero<R>() : s.acc[c * cs + idx];
+    }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const size_t i = c * cs + idx;
-      const C2<R> u = s.u[i];
-      const C2<R> st = first ? u : s.temp[i];
-      const C2<R> rhs = cmk<R>(nl[c].x + visc * st.x, nl[c].y + visc * st.y);
+      const C2<R> rhs = cmk<R>(nl[c].x + visc * st[c].x, nl[c].y + visc * st[c].y);
       if (s.op == ST_RK4_1) {
         s.acc[i] = rhs;
-        s.temp[i] = cmk<R>(u.x + half * rhs.x, u.y + half * rhs.y);
+        s.temp[i] = cmk<R>(u[c].x + half * rhs.x, u[c].y + half * rhs.y);
       } else if (s.op == ST_RK4_2 || s.op == ST_RK4_3) {
-        const C2<R> a = s.acc[i];
-        s.acc[i] = cmk<R>(a.x + R(2) * rhs.x, a.y + R(2) * rhs.y);
+        s.acc[i] = cmk<R>(a[c].x + R(2) * rhs.x, a[c].y + R(2) * rhs.y);
         const R h = s.op == ST_RK4_2 ? half : (R)dt;
-        s.temp[i] = cmk<R>(u.x + h * rhs.x, u.y + h * rhs.y);
+        s.temp[i] = cmk<R>(u[c].x + h * rhs.x, u[c].y + h * rhs.y);
       } else {
-        const C2<R> a = s.acc[i];
         const R sixth = (R)(dt / 6.0);
-        s.u[i] = cmk<R>(u.x + sixth * (a.x + rhs.x), u.y + sixth * (a.y + rhs.y));
+        s.u[i] = cmk<R>(u[c].x + sixth * (a[c].x + rhs.x), u[c].y + sixth * (a[c].y + rhs.y));
       }
     }
     return;
   }
   const double* e = s.etd + (size_t)m * ETD_STRIDE;
+  switch (s.op) {
+    case ST_ETD_REF_1: {  // solver.rs:264-281
+      const R eh = (R)e[E_HALF], q = (R)(dt * e[E_A21]);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const size_t i = c * cs + idx;
-    const C2<R> u = s.u[i];
-    const C2<R> n = nl[c];
-    switch (s.op) {
-      case ST_ETD_REF_1: {  // solver.rs:264-281
-        s.n1[i] = n;
-        s.temp[i] = axpby<R>((R)e[E_HALF], u, (R)(dt * e[E_A21]), n);
-        break;
+      for (int c = 0; c < 3; ++c) {
+        s.n1[c * cs + idx] = nl[c];
+        s.temp[c * cs + idx] = axpby<R>(eh, u[c], q, nl[c]);
       }
-      case ST_ETD_REF_2: {  // solver.rs:291-308; acc starts the final sum
-        const C2<R> n1 = s.n1[i];
-        s.acc[i] = axpby<R>((R)e[E_B1], n1, (R)e[E_B23], n);
-        s.temp[i] = axpby<R>((R)e[E_HALF], u, (R)(dt * e[E_A21]), n);
-        break;
-      }
-      case ST_ETD_REF_3: {  // solver.rs:318-344
-        const C2<R> n1 = s.n1[i];
-        const C2<R> a = s.acc[i];
-        const R b23 = (R)e[E_B23];
-        s.acc[i] = cmk<R>(a.x + b23 * n.x, a.y + b23 * n.y);
-        const C2<R> dn = cmk<R>(R(2) * n.x - n1.x, R(2) * n.y - n1.y);
-        s.temp[i] = axpby<R>((R)e[E_FULL], u, (R)(dt * e[E_A41]), dn);
-        break;
-      }
-      case ST_ETD_4: {  // solver.rs:354-378
-        const C2<R> a = s.acc[i];
-        const R b4 = (R)e[E_B4];
-        const C2<R> rhs = cmk<R>(a.x + b4 * n.x, a.y + b4 * n.y);
-        s.u_out[i] = axpby<R>((R)e[E_FULL], u, (R)dt, rhs);
-        break;
-      }
-      case ST_ETD_CM_1: {  // textbook: a = E2 u + (h/2) phi1(z/2) N1
-        s.n1[i] = n;
-        s.temp[i] = axpby<R>((R)e[E_HALF], u, (R)(0.5 * dt * e[E_A21]), n);
-        break;
-      }
-      case ST_ETD_CM_2: {  // b = E2 u + (h/2) phi1(z/2) N2
-        const C2<R> n1 = s.n1[i];
-        s.acc[i] = axpby<R>((R)e[E_B1], n1, (R)e[E_B23], n);
-        s.temp[i] = axpby<R>((R)e[E_HALF], u, (R)(0.5 * dt * e[E_A21]), n);
-        break;
-      }
-      case ST_ETD_CM_3: {  // c = E2 a + (h/2) phi1(z/2) (2 N3 - N1), a rebuilt from u, N1
-        const C2<R> n1 = s.n1[i];
-        const C2<R> ac = s.acc[i];
-        const R b23 = (R)e[E_B23];
-        s.acc[i] = cmk<R>(ac.x + b23 * n.x, ac.y + b23 * n.y);
-        const R eh = (R)e[E_HALF];
-        const R q = (R)(0.5 * dt * e[E_A21]);
-        const C2<R> a = axpby<R>(eh, u, q, n1);
-        const C2<R> dn = cmk<R>(R(2) * n.x - n1.x, R(2) * n.y - n1.y);
-        s.temp[i] = axpby<R>(eh, a, q, dn);
-        break;
-      }
-      default: break;
+      break;
     }
+    case ST_ETD_REF_2: {  // solver.rs:291-308; acc starts the final sum
+      const R b1 = (R)e[E_B1], b23 = (R)e[E_B23], eh = (R)e[E_HALF], q = (R)(dt * e[E_A21]);
+      C2<R> n1[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) n1[c] = s.n1[c * cs + idx];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        s.acc[c * cs + idx] = axpby<R>(b1, n1[c], b23, nl[c]);
+        s.temp[c * cs + idx] = axpby<R>(eh, u[c], q, nl[c]);
+      }
+      break;
+    }
+    case ST_ETD_REF_3: {  // solver.rs:318-344
+      const R b23 = (R)e[E_B23], ef = (R)e[E_FULL], q = (R)(dt * e[E_A41]);
+      C2<R> n1[3], a[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        n1[c] = s.n1[c * cs + idx];
+        a[c] = s.acc[c * cs + idx];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        s.acc[c * cs + idx] = cmk<R>(a[c].x + b23 * nl[c].x, a[c].y + b23 * nl[c].y);
+        const C2<R> dn = cmk<R>(R(2) * nl[c].x - n1[c].x, R(2) * nl[c].y - n1[c].y);
+        s.temp[c * cs + idx] = axpby<R>(ef, u[c], q, dn);
+      }
+      break;
+    }
+    case ST_ETD_4: {  // solver.rs:354-378
+      const R b4 = (R)e[E_B4], ef = (R)e[E_FULL];
+      C2<R> a[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) a[c] = s.acc[c * cs + idx];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const C2<R> rhs = cmk<R>(a[c].x + b4 * nl[c].x, a[c].y + b4 * nl[c].y);
+        s.u_out[c * cs + idx] = axpby<R>(ef, u[c], (R)dt, rhs);
+      }
+      break;
+    }
+    case ST_ETD_CM_1: {  // textbook: a = E2 u + (h/2) phi1(z/2) N1
+      const R eh = (R)e[E_HALF], q = (R)(0.5 * dt * e[E_A21]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        s.n1[c * cs + idx] = nl[c];
+        s.temp[c * cs + idx] = axpby<R>(eh, u[c], q, nl[c]);
+      }
+      break;
+    }
+    case ST_ETD_CM_2: {  // b = E2 u + (h/2) phi1(z/2) N2
+      const R b1 = (R)e[E_B1], b23 = (R)e[E_B23], eh = (R)e[E_HALF], q = (R)(0.5 * dt * e[E_A21]);
+      C2<R> n1[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) n1[c] = s.n1[c * cs + idx];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        s.acc[c * cs + idx] = axpby<R>(b1, n1[c], b23, nl[c]);
+        s.temp[c * cs + idx] = axpby<R>(eh, u[c], q, nl[c]);
+      }
+      break;
+    }
+    case ST_ETD_CM_3: {  // c = E2 a + (h/2) phi1(z/2) (2 N3 - N1), a rebuilt from u, N1
+      const R b23 = (R)e[E_B23], eh = (R)e[E_HALF], q = (R)(0.5 * dt * e[E_A21]);
+      C2<R> n1[3], ac[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        n1[c] = s.n1[c * cs + idx];
+        ac[c] = s.acc[c * cs + idx];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        s.acc[c * cs + idx] = cmk<R>(ac[c].x + b23 * nl[c].x, ac[c].y + b23 * nl[c].y);
+        const C2<R> a = axpby<R>(eh, u[c], q, n1[c]);
+        const C2<R> dn = cmk<R>(R(2) * nl[c].x - n1[c].x, R(2) * nl[c].y - n1[c].y);
+        s.temp[c * cs + idx] = axpby<R>(eh, a, q, dn);
+      }
+      break;
+    }
+    default: break;
   }
 }
 

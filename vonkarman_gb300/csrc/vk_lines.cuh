@@ -41,19 +41,25 @@ __host__ __device__ constexpr int rplan_radix_f(int L, int s) {
        : L == 768 ? (s == 0 ? 32 : 24)
        : 1;
 }
-template <typename R> __host__ __device__ constexpr int rstages(int L) {
+// Contiguous lines (z passes) keep the radix-16 stage first where the
+// larger radix would put the first-stage writes (stride RAD positions) on
+// shared-memory banks that the one-slot-per-128-bytes padding cannot spread.
+__host__ __device__ constexpr int rplan_radix_fc(int L, int s) {
+  return L == 384 ? (s == 0 ? 16 : 24) : rplan_radix_f(L, s);
+}
+template <typename R, bool CONTIG = false> __host__ __device__ constexpr int rstages(int L) {
   return sizeof(R) == 4 ? rplan_stages_f(L) : plan_stages(L);
 }
-template <typename R> __host__ __device__ constexpr int rradix(int L, int s) {
-  return sizeof(R) == 4 ? rplan_radix_f(L, s) : plan_radix(L, s);
+template <typename R, bool CONTIG = false> __host__ __device__ constexpr int rradix(int L, int s) {
+  return sizeof(R) == 4 ? (CONTIG ? rplan_radix_fc(L, s) : rplan_radix_f(L, s)) : plan_radix(L, s);
 }
 // threads of a CTA: one butterfly per thread in the widest stage
-template <typename R, int L, int NLINES, int S = 0>
+template <typename R, int L, int NLINES, bool CONTIG = false, int S = 0>
 __host__ __device__ constexpr int rthreads() {
-  if constexpr (S >= rstages<R>(L)) {
+  if constexpr (S >= rstages<R, CONTIG>(L)) {
     return 32;
   } else {
-    return cmax(round32(L / rradix<R>(L, S) * NLINES), rthreads<R, L, NLINES, S + 1>());
+    return cmax(round32(L / rradix<R, CONTIG>(L, S) * NLINES), rthreads<R, L, NLINES, CONTIG, S + 1>());
   }
 }
 // FP32 with 8 lines: the first stage writes at stride RAD0 positions, so a
@@ -83,7 +89,8 @@ __host__ __device__ constexpr int lines_min_blocks() {
   if constexpr (sizeof(R) == 8) {
     return L >= 512 ? 1 : cmax(1, 768 / NT);
   } else {
-    return L >= 768 ? (EPI ? 1 : 2) : EPI ? cmax(1, 512 / NT) : NT < 128 ? 4 : cmax(1, 768 / NT);
+    return L >= 768 ? (EPI ? 1 : 2) : EPI ? cmax(1, 512 / NT) : L >= 512 ? 2 : L >= 384 ? 3
+         : NT < 128 ? 4 : cmax(1, 768 / NT);
   }
 }
 
@@ -92,6 +99,7 @@ __host__ __device__ constexpr int lines_min_blocks() {
 // consecutive lanes take consecutive lines, so every thread keeps one line.
 template <typename R, int L, int NLINES>
 struct MapInterleaved {
+  static constexpr bool CONTIG = false;
   template <int NB> __device__ __forceinline__ static int line(int g) { return g % NLINES; }
   template <int NB> __device__ __forceinline__ static int bfly(int g) { return g / NLINES; }
   template <int S> __device__ __forceinline__ static int idx(int pos, int l) { return ridx<R, L, NLINES, S>(pos, l); }
@@ -102,6 +110,7 @@ struct MapInterleaved {
 // butterflies of a line, so global accesses along a line coalesce.
 template <typename R, int L, int NLINES>
 struct MapContig {
+  static constexpr bool CONTIG = true;
   template <int NB> __device__ __forceinline__ static int line(int g) { return g / NB; }
   template <int NB> __device__ __forceinline__ static int bfly(int g) { return g % NB; }
   template <int S> __device__ __forceinline__ static int idx(int pos, int l) { return l * zpad_len<R>(L) + zi<R>(pos); }
@@ -110,29 +119,55 @@ struct MapContig {
 
 template <typename R, int L, bool INV, int NT, int NLINES, class MAP, int S, int NS>
 struct RegStage {
-  static constexpr int RAD = rradix<R>(L, S);
+  static constexpr int RAD = rradix<R, MAP::CONTIG>(L, S);
   static constexpr int NB = L / RAD;            // butterflies per line
   static constexpr int G = NB * NLINES;         // butterflies per stage
   static constexpr int Q = (G + NT - 1) / NT;
-  static constexpr bool LAST = S + 1 == rstages<R>(L);
+  static constexpr bool LAST = S + 1 == rstages<R, MAP::CONTIG>(L);
   static constexpr int TWS = L / (NS * RAD);    // twiddle table stride
 
-  // ld(l, p) -> input position p of line l; st(l, p, v) takes output p.
-  template <class LD, class ST>
-  __device__ __forceinline__ static void run(C2<R>* xb, const C2<R>* __restrict__ tw, const LD& ld,
+  // ld(l, p) -> raw input of position p of line l (memory loads only),
+  // pp(l, p, raw) -> the complex input (arithmetic on the loaded values),
+  // st(l, p, v) takes output p.  All loads of the first stage are issued
+  // before any arithmetic on them: in-order issue would otherwise wait on each
+  // load before issuing the next.
+  template <class LD, class PP, class ST>
+  __device__ __forceinline__ static void run(C2<R>* xb, const C2<R>* __restrict__ tw, const LD& ld, const PP& pp,
                                              const ST& st) {
     const int tid = threadIdx.x;
     C2<R> v[Q][RAD];
+    if constexpr (S == 0) {
+      // raw inputs wider than one complex value are staged in chunks of
+      // 192 (FP32) / 128 (FP64) bytes per thread (registers)
+      using Raw = decltype(ld(0, 0));
+      constexpr int CH = sizeof(Raw) > sizeof(C2<R>) ? cmin(RAD, (int)((sizeof(R) == 4 ? 192 : 128) / sizeof(Raw))) : RAD;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int g = tid + q * NT;
-      if (G % NT == 0 || g < G) {
-        const int l = MAP::template line<NB>(g);
-        const int j = MAP::template bfly<NB>(g);
-        if constexpr (S == 0) {
+      for (int q = 0; q < Q; ++q) {
+        const int g = tid + q * NT;
+        if (G % NT == 0 || g < G) {
+          const int l = MAP::template line<NB>(g);
+          const int j = MAP::template bfly<NB>(g);
 #pragma unroll
-          for (int r = 0; r < RAD; ++r) v[q][r] = ld(l, j + r * NB);
-        } else {
+          for (int r0 = 0; r0 < RAD; r0 += CH) {
+            Raw raw[CH];
+#pragma unroll
+            for (int r = 0; r < CH; ++r) {
+              if (r0 + r < RAD) raw[r] = ld(l, j + (r0 + r) * NB);
+            }
+#pragma unroll
+            for (int r = 0; r < CH; ++r) {
+              if (r0 + r < RAD) v[q][r0 + r] = pp(l, j + (r0 + r) * NB, raw[r]);
+            }
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int g = tid + q * NT;
+        if (G % NT == 0 || g < G) {
+          const int l = MAP::template line<NB>(g);
+          const int j = MAP::template bfly<NB>(g);
 #pragma unroll
           for (int r = 0; r < RAD; ++r) v[q][r] = xb[MAP::template idx<S - 1>(j + r * NB, l)];
         }
@@ -165,7 +200,7 @@ struct RegStage {
     }
     if constexpr (!LAST) {
       __syncthreads();
-      RegStage<R, L, INV, NT, NLINES, MAP, S + 1, NS * RAD>::run(xb, tw, ld, st);
+      RegStage<R, L, INV, NT, NLINES, MAP, S + 1, NS * RAD>::run(xb, tw, ld, pp, st);
     }
   }
 };
@@ -174,18 +209,28 @@ struct RegStage {
 // xb (MAP::elems() elements) must not be in use by any thread.  Returns with
 // no synchronisation after the last stage.
 template <typename R, int L, bool INV, int NT, int NLINES, class MAP = MapInterleaved<R, L, NLINES>, class LD,
-          class ST>
-__device__ __forceinline__ void fft_lines(C2<R>* xb, const C2<R>* __restrict__ tw, const LD& ld, const ST& st) {
+          class PP, class ST>
+__device__ __forceinline__ void fft_lines(C2<R>* xb, const C2<R>* __restrict__ tw, const LD& ld, const PP& pp,
+                                          const ST& st) {
   static_assert(rstages<R>(L) > 0, "unsupported FFT length");
-  RegStage<R, L, INV, NT, NLINES, MAP, 0, 1>::run(xb, tw, ld, st);
+  RegStage<R, L, INV, NT, NLINES, MAP, 0, 1>::run(xb, tw, ld, pp, st);
 }
+// pp for inputs that need no arithmetic after the load
+struct PrepNone {
+  template <class T> __device__ __forceinline__ T operator()(int, int, const T& v) const { return v; }
+};
 
 // Generic strided pass: NLINES consecutive lines lam = outer * hz + z of one
 // field per CTA (blockIdx.x = f + nfields * tile), so no z tile is partly
-// empty.  Op supplies load(f, outer, z, p), out_index(p) (-1: dropped) and
-// store(f, outer, z, i, v).
+// empty.  Op supplies kind(f) in [0, NKIND) (fields of one kind share their
+// load/prep code, which is specialised per kind), load<K>(f, outer, z, p)
+// (memory loads only, zero for padded positions), prep<K>(f, outer, z, p,
+// raw), staged<K>() (stage the combined inputs in shared memory first),
+// out_index(p) (-1: dropped) and store(f, outer, z, i, v).  Lines past the
+// end (lam >= nlines) load line 0 and store nothing.
 template <typename R, int L, bool INV, int NLINES, int NT, class Op>
 __global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op op, const C2<R>* __restrict__ tw, int nlines) {
+  static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   const int f = blockIdx.x % op.nfields;
@@ -194,13 +239,58 @@ __global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op o
   const bool ok = lam < nlines;
   const int outer = ok ? lam / op.hz : 0;
   const int z = ok ? lam - outer * op.hz : 0;
-  static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
-  fft_lines<R, L, INV, NT, NLINES>(
-      xb, tw, [&](int, int p) { return ok ? op.load(f, outer, z, p) : czero<R>(); },
-      [&](int, int p, C2<R> v) {
-        const int i = op.out_index(p);
-        if (ok && i >= 0) op.store(f, outer, z, i, v);
-      });
+  const int kd = op.kind(f);
+  auto st = [&](int, int p, C2<R> v) {
+    const int i = op.out_index(p);
+    if (ok && i >= 0) op.store(f, outer, z, i, v);
+  };
+  sfor<Op::NKIND>([&](auto kc) {
+    constexpr int K = decltype(kc)::value;
+    if (kd != K) return;   // uniform over the CTA
+    if constexpr (Op::template staged<K>()) {
+      // Inputs that combine several loads per position: every thread loads
+      // its share of the tile (positions tid / NLINES + i NT / NLINES of its
+      // own line), combines, and stages the result in shared memory; the
+      // first stage then reads shared memory.
+      C2<R>* sin = xb + rsmem_elems<R, L, NLINES>();
+      constexpr int PER = (L * NLINES + NT - 1) / NT;
+      const int l = threadIdx.x % NLINES;
+      using Raw = decltype(op.template load<K>(f, outer, z, 0));
+      Raw raw[PER];
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const int p = (int)threadIdx.x / NLINES + i * (NT / NLINES);
+        if (p < L) raw[i] = op.template load<K>(f, outer, z, p);
+      }
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const int p = (int)threadIdx.x / NLINES + i * (NT / NLINES);
+        if (p < L) sin[p * NLINES + l] = op.template prep<K>(f, outer, z, p, raw[i]);
+      }
+      __syncthreads();
+      fft_lines<R, L, INV, NT, NLINES>(
+          xb, tw, [&](int ll, int p) { return sin[p * NLINES + ll]; }, PrepNone{}, st);
+    } else {
+      fft_lines<R, L, INV, NT, NLINES>(
+          xb, tw, [&](int, int p) { return op.template load<K>(f, outer, z, p); },
+          [&](int, int p, const auto& raw) { return op.template prep<K>(f, outer, z, p, raw); }, st);
+    }
+  });
+}
+// shared memory of k_lines: the exchange buffer, plus a staging tile when a
+// field of this launch has a staged kind
+template <int K, class Op> inline bool kind_staged(int k) {
+  if constexpr (K >= Op::NKIND) {
+    return false;
+  } else {
+    return k == K ? Op::template staged<K>() : kind_staged<K + 1, Op>(k);
+  }
+}
+template <typename R, int L, int NLINES, class Op>
+inline size_t lines_smem_bytes(const Op& op) {
+  bool staged = false;
+  for (int f = 0; f < op.nfields; ++f) staged = staged || kind_staged<0, Op>(op.kind(f));
+  return (size_t)(rsmem_elems<R, L, NLINES>() + (staged ? L * NLINES : 0)) * sizeof(C2<R>);
 }
 
 // ---------------------------------------------------------------------------
@@ -239,7 +329,7 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
       if (C > 0) __syncthreads();   // xb is reused
       const C2<R>* src = a.in + (size_t)C * a.fsin + (size_t)iy * H + z;
       fft_lines<R, L, false, NT, NLINES>(
-          xb, tw, [&](int, int p) { return ok ? src[(size_t)p * N * H] : czero<R>(); },
+          xb, tw, [&](int, int p) { return src[(size_t)p * N * H]; }, PrepNone{},
           [&](int, int p, C2<R> v) {
             const int ix = unpad_pos(p, N, L);
             if (ix >= 0) keep[(C * N + ix) * NLINES + (int)(threadIdx.x % NLINES)] = v;
@@ -285,7 +375,7 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
 // ---------------------------------------------------------------------------
 template <typename R, int M, int CP>
 __host__ __device__ constexpr int p3_threads() {
-  return cmin(rthreads<R, M, 6 * CP>(), 384);
+  return cmin(rthreads<R, M, 6 * CP, true>(), 384);
 }
 
 template <typename R, int M, int CP, int NT>
@@ -301,18 +391,22 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
   const int col0 = blockIdx.x * 2 * CP;
   fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>>(
       A, tw,
-      [&](int l, int p) -> C2<R> {
+      [&](int l, int p) -> C2x2<R> {
         const int t = l / (2 * CP);
         const int col = col0 + l % (2 * CP);
-        if (col >= a.ncols) return czero<R>();
         const bool lo = p < H;
-        if (!lo && p <= M - H) return czero<R>();
-        const int k = lo ? p : M - p;
-        const C2<R>* src = a.in + (size_t)col * H + k;
-        const C2<R> X = src[(size_t)(2 * t) * a.fsin];
-        const C2<R> Y = src[(size_t)(2 * t + 1) * a.fsin];
+        C2x2<R> r{};
+        if (col < a.ncols && (lo || p > M - H)) {
+          const C2<R>* src = a.in + (size_t)col * H + (lo ? p : M - p);
+          r.a = src[(size_t)(2 * t) * a.fsin];
+          r.b = src[(size_t)(2 * t + 1) * a.fsin];
+        }
+        return r;
+      },
+      [&](int, int p, const C2x2<R>& r) -> C2<R> {   // Z = X + i Y with the Hermitian extension
+        const C2<R> X = r.a, Y = r.b;
         if (p == 0) return cmk<R>(X.x, Y.x);
-        return lo ? cmk<R>(X.x - Y.y, X.y + Y.x) : cmk<R>(X.x + Y.y, Y.x - X.y);
+        return p < H ? cmk<R>(X.x - Y.y, X.y + Y.x) : cmk<R>(X.x + Y.y, Y.x - X.y);
       },
       [&](int l, int p, C2<R> v) { B[l * LP + zi<R>(p)] = v; });
   __syncthreads();
@@ -335,7 +429,7 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
   }
   __syncthreads();
   fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>>(
-      B, tw, [&](int l, int p) { return A[l * LP + zi<R>(p)]; },
+      B, tw, [&](int l, int p) { return A[l * LP + zi<R>(p)]; }, PrepNone{},
       [&](int l, int p, C2<R> v) { A[l * LP + zi<R>(p)] = v; });
   __syncthreads();
   for (int e = threadIdx.x; e < CP * 3 * H; e += NT) {

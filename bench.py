@@ -186,12 +186,12 @@ def step_bytes(n: int, elem: int) -> float:
     return per * elem
 
 
-# DRAM traffic (read + write bytes) of one launch from the committed ncu
-# captures (profiles/k_p3_*_isotropic_n128.md), taken at N=128 and scaled to a
-# full launch at grid n by the number of padded columns x modes (M^2 H).
+# DRAM traffic (read + write bytes) of one launch of the dominant kernel from
+# ncu captures (dram__bytes_read.sum + dram__bytes_write.sum): FP64 at N=128,
+# FP32-bulk at N=256, scaled to grid n by the padded columns x modes (M^2 H).
 NCU_TRAFFIC = {
     ("P3_z_c2r_cross_r2c", "fp64"): (128, 230115840 + 85875200),
-    ("P3_z_c2r_cross_r2c", "fp32bulk"): (128, 115037952 + 29144576),
+    ("P3_z_c2r_cross_r2c", "fp32bulk"): (256, 913084160 + 426719744),
 }
 
 
@@ -486,7 +486,7 @@ def run_ours(args, d: Dist):
         "hbm_gbs_step": sb / (ms / args.steps * 1e-3) / 1e9,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": scaled_traffic(dom, args.precision, n),
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at N=128, scaled by M^2 H",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (FP64: N=128 scaled by M^2 H; FP32-bulk: N=256)",
                      "peak_source": hbm_src,
                      "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
         "fp64_roofline": {"kernel": dom, "achieved": dom_gflops, "peak": fp64_peak, "unit": "GFLOP/s",

@@ -206,6 +206,33 @@ def test_one_step_taylor_green_n64_fixed_dt(vk):
     assert s.time() == pytest.approx(dt, rel=0, abs=0)
 
 
+def test_taylor_green_n64_100_steps_tier1_and_spectrum_vs_golden(vk):
+    # the CPU-runnable Taylor-Green case over its 100 steps: Tier-1 after every
+    # step within 1e-10 relative, E(k) at step 100 (golden fixture made by the
+    # oracle, tests/golden/make_golden.py)
+    import os
+
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "tg64_fixed.npz"))
+    n, nu, dt = int(z["n"]), float(z["nu"]), float(z["dt"])
+    keys = [str(k) for k in z["keys"]]
+    s = vk.Periodic3D(vk.GridSpec(n), nu, vo.taylor_green(vo.Grid(n)),
+                      vk.SolverOptions(dt_mode="fixed", dt_fixed=dt))
+    recs = s.run(100, every=1)
+    assert len(recs) == 100
+    scale = float(z["tier1"][0, keys.index("enstrophy")])
+    for i, r in enumerate(recs):
+        for j, k in enumerate(keys):
+            ref = float(z["tier1"][i + 1, j])
+            got = float(getattr(r, k))
+            # helicity-type values of Taylor-Green are zero up to rounding: an
+            # absolute floor of 1e-10 x the enstrophy scale
+            tol = max(TOL_DIAG * abs(ref), TOL_DIAG * scale if "helicity" in k else 0.0)
+            assert abs(got - ref) <= tol, (i + 1, k, got, ref)
+    shells, spec = vk.energy_spectrum(s)
+    assert np.array_equal(shells, z["shells"])
+    assert np.abs(spec - z["spectrum"]).max() <= TOL_DIAG * np.abs(z["spectrum"]).max()
+
+
 @pytest.mark.parametrize("n", [16, 32])
 def test_steps_random_cfl_vs_oracle(vk, n):
     g = vo.Grid(n)

@@ -21,16 +21,58 @@
 
 namespace vk {
 
-// A1: fields 0..4 as P1 on x; fields 5..7 = Pad(mul * S_out * P nbar / w_M).
-// Kinds: 0 = u_c, 1 = i kx u, 2 = c_bar (Leray projection and ETD factor
-// applied at the load, three loads per position).
+// c_bar source of A1 (elementwise over the N-grid modes, before A1):
+// cb = mul * S_out * P nbar / w_M with mul = fac dt etd[slot] (slot >= 0),
+// P the Leray projection (spectral_ops.rs:114-151) and the padded-grid R2C
+// weight 1/w_M (1 at kz = 0, 1/2 elsewhere: the N-grid Nyquist plane is
+// interior on the padded grid).
+template <typename R> struct CbarArgs {
+  int N, H;
+  R s_cbar, ks;
+  const C2<R>* nb; size_t cs;
+  const double* etd; int slot; double fac; const double* dt;
+  C2<R>* out;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_adj_cbar(CbarArgs<R> a) {
+  const size_t total = (size_t)a.N * a.N * a.H;
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const int z = (int)(idx % a.H);
+  const size_t r = idx / a.H;
+  const int iy = (int)(r % a.N), ix = (int)(r / a.N);
+  C2<R> b[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) b[j] = a.nb[(size_t)j * a.cs + idx];
+  const int kxi = signed_k(ix, a.N), kyi = signed_k(iy, a.N);
+  R mul = a.s_cbar * (z == 0 ? R(1) : R(0.5));
+  if (a.slot >= 0) {
+    const int m = kxi * kxi + kyi * kyi + z * z;
+    mul *= (R)(a.fac * (*a.dt) * a.etd[(size_t)m * ETD_STRIDE + a.slot]);
+  }
+  const R kx = a.ks * (R)kxi, ky = a.ks * (R)kyi, kz = a.ks * (R)z;
+  const R k2 = (kx * kx + ky * ky) + kz * kz;
+  C2<R> v[3] = {b[0], b[1], b[2]};
+  if (!(k2 < R(1e-30))) {
+    const R inv = R(1) / k2;
+    const C2<R> kd = cmk<R>((kx * b[0].x + ky * b[1].x) + kz * b[2].x, (kx * b[0].y + ky * b[1].y) + kz * b[2].y);
+    v[0] = cmk<R>(b[0].x - kx * kd.x * inv, b[0].y - kx * kd.y * inv);
+    v[1] = cmk<R>(b[1].x - ky * kd.x * inv, b[1].y - ky * kd.y * inv);
+    v[2] = cmk<R>(b[2].x - kz * kd.x * inv, b[2].y - kz * kd.y * inv);
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) a.out[(size_t)j * a.cs + idx] = cscale<R>(v[j], mul);
+}
+
+// A1: fields 0..4 as P1 on x; fields 5..7 = x-inverse of Pad(c_bar source)
+// (k_adj_cbar).  Kinds: 0 = u_c, 1 = i kx u, 2 = c_bar.
 template <typename R> struct OpAdjXInv {
   int nfields, hz;
   int N, M;
-  R s_in, s_cbar, ks;
+  R s_in, ks;
   const C2<R>* in; size_t cs;          // stage input x
-  const C2<R>* nb;                     // cotangent source (3 components, stride cs)
-  const double* etd; int slot; double fac; const double* dt;   // mul = fac dt etd[slot] if slot >= 0
+  const C2<R>* cb;                     // c_bar source (3 components, stride cs)
   C2<R>* out; size_t fs;
   static constexpr bool STAGED_ANY = false;
   template <int K> __host__ __device__ static constexpr bool staged() { return false; }
@@ -38,33 +80,9 @@ template <typename R> struct OpAdjXInv {
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : f < 5 ? 1 : 2; }
   template <int K> __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
     const int ix = unpad_pos(p, N, M);
-    if constexpr (K < 2) {
-      const int c = K == 0 ? f : f - 2;
-      return ix < 0 ? czero<R>() : in[(size_t)c * cs + ((size_t)ix * N + iy) * hz + z];
-    } else {
-      if (ix < 0) return czero<R>();
-      const size_t idx = ((size_t)ix * N + iy) * hz + z;
-      const int kxi = signed_k(ix, N), kyi = signed_k(iy, N);
-      const int c = f - 5;
-      C2<R> b[3];
-#pragma unroll
-      for (int j = 0; j < 3; ++j) b[j] = nb[(size_t)j * cs + idx];
-      const R kx = ks * (R)kxi, ky = ks * (R)kyi, kz = ks * (R)z;
-      const R k2 = (kx * kx + ky * ky) + kz * kz;
-      C2<R> v = b[c];
-      if (!(k2 < R(1e-30))) {
-        const R inv = R(1) / k2;
-        const C2<R> kd = cmk<R>((kx * b[0].x + ky * b[1].x) + kz * b[2].x, (kx * b[0].y + ky * b[1].y) + kz * b[2].y);
-        const R kc = c == 0 ? kx : c == 1 ? ky : kz;
-        v = cmk<R>(v.x - kc * kd.x * inv, v.y - kc * kd.y * inv);
-      }
-      R mul = s_cbar * (z == 0 ? R(1) : R(0.5));
-      if (slot >= 0) {
-        const int m = kxi * kxi + kyi * kyi + z * z;
-        mul *= (R)(fac * (*dt) * etd[(size_t)m * ETD_STRIDE + slot]);
-      }
-      return cscale<R>(v, mul);
-    }
+    const C2<R>* src = K == 2 ? cb : in;
+    const int c = K == 0 ? f : K == 1 ? f - 2 : f - 5;
+    return ix < 0 ? czero<R>() : src[(size_t)c * cs + ((size_t)ix * N + iy) * hz + z];
   }
   template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int p, C2<R> v) const {
     if constexpr (K == 2) {
@@ -130,95 +148,93 @@ template <typename R> struct A3Args {
   C2<R>* out; size_t fsout;         // 6 fields (M, M, H)
 };
 
+template <typename R, int M, int CP>
+__host__ __device__ constexpr int adj_z_threads() {
+  return cmin(rthreads<R, M, 9 * CP, true>(), 384);
+}
+// Shared memory of k_adj_z: 9 CP inverse lines (exchange, then the physical
+// values in place) and 6 CP forward lines.
+template <typename R, int M, int CP>
+__host__ __device__ constexpr int adj_z_smem_elems() {
+  return 15 * CP * zpad_len<R>(M);
+}
+
+// On the register engine: inverse lines l < 8 CP are the packed pair
+// t = l / 2CP of column c = l % 2CP; lines 8 CP + pr carry c_bar_z of the two
+// columns of pair pr.  Forward lines l = t * 2CP + c: (ab_x + i ab_y),
+// (ab_z + i ob_x), (ob_y + i ob_z) of column c.
 template <typename R, int M, int CP, int NT>
-__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_adj_z(A3Args<R> a, const C2<R>* __restrict__ tw) {
+__global__ void __launch_bounds__(NT, M >= 768 ? 1 : cmax(1, (sizeof(R) == 8 ? 768 : 512) / NT))
+k_adj_z(A3Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int N = 2 * M / 3;
   constexpr int H = N / 2 + 1;
-  constexpr int NL = 9 * CP;
   constexpr int LP = zpad_len<R>(M);
+  constexpr int NI = 9 * CP, NF = 6 * CP;
   extern __shared__ __align__(16) unsigned char vk_smem[];
-  C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
+  C2<R>* A = reinterpret_cast<C2<R>*>(vk_smem);   // NI lines
+  C2<R>* B = A + NI * LP;                          // NF lines
   const int col0 = blockIdx.x * 2 * CP;
-  constexpr int TOT = 2 * CP * 4 * H;
-  constexpr int PER = (TOT + NT - 1) / NT;
-  C2<R> lx[PER], ly[PER];
+  fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>, true>(
+      A, tw,
+      [&](int l, int p) -> C2x2<R> {
+        int fx, fy, cx, cy;
+        if (l < 8 * CP) {
+          const int t = l / (2 * CP);
+          fx = 2 * t; fy = 2 * t + 1;
+          cx = cy = col0 + l % (2 * CP);
+        } else {
+          fx = fy = 8;
+          cx = col0 + 2 * (l - 8 * CP);
+          cy = cx + 1;
+        }
+        const bool lo = p < H;
+        C2x2<R> r{};
+        if (lo || p > M - H) {
+          const int k = lo ? p : M - p;
+          if (cx < a.ncols) r.a = a.in[(size_t)fx * a.fsin + (size_t)cx * H + k];
+          if (cy < a.ncols) r.b = a.in[(size_t)fy * a.fsin + (size_t)cy * H + k];
+        }
+        return r;
+      },
+      [&](int, int p, const C2x2<R>& r) -> C2<R> {   // Z = X + i Y with the Hermitian extension
+        const C2<R> X = r.a, Y = r.b;
+        if (p == 0) return cmk<R>(X.x, Y.x);
+        return p < H ? cmk<R>(X.x - Y.y, X.y + Y.x) : cmk<R>(X.x + Y.y, Y.x - X.y);
+      },
+      [&](int l, int p, C2<R> v) { A[l * LP + zi<R>(p)] = v; });
+  __syncthreads();
+  for (int e = threadIdx.x; e < CP * M; e += NT) {
+    const int pr = e / M, p = e % M;
+    const int zp = zi<R>(p);
+    const C2<R> Z = A[(8 * CP + pr) * LP + zp];
 #pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int e = threadIdx.x + q * NT;
+    for (int cc = 0; cc < 2; ++cc) {
+      const int c = 2 * pr + cc;
+      const C2<R> z0 = A[c * LP + zp], z1 = A[(2 * CP + c) * LP + zp], z2 = A[(4 * CP + c) * LP + zp],
+                  z3 = A[(6 * CP + c) * LP + zp];
+      const R ux = z0.x, uy = z0.y, uz = z1.x, wx = z1.y, wy = z2.x, wz = z2.y;
+      const R cx = z3.x, cy = z3.y, cz = cc == 0 ? Z.x : Z.y;
+      // a_bar = w x cb ; o_bar = cb x u
+      const R abx = wy * cz - wz * cy, aby = wz * cx - wx * cz, abz = wx * cy - wy * cx;
+      const R obx = cy * uz - cz * uy, oby = cz * ux - cx * uz, obz = cx * uy - cy * ux;
+      B[c * LP + zp] = cmk<R>(abx, aby);
+      B[(2 * CP + c) * LP + zp] = cmk<R>(abz, obx);
+      B[(4 * CP + c) * LP + zp] = cmk<R>(oby, obz);
+    }
+  }
+  __syncthreads();
+  fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>>(
+      A, tw, [&](int l, int p) { return B[l * LP + zi<R>(p)]; }, PrepNone{},
+      [&](int l, int p, C2<R> v) { B[l * LP + zi<R>(p)] = v; });
+  __syncthreads();
+  for (int e = threadIdx.x; e < 2 * CP * 3 * H; e += NT) {
     const int k = e % H;
-    const int t = (e / H) % 4;
-    const int col = col0 + e / (4 * H);
-    const bool ok = e < TOT && col < a.ncols;
-    lx[q] = ok ? a.in[(size_t)(2 * t) * a.fsin + (size_t)col * H + k] : czero<R>();
-    ly[q] = ok ? a.in[(size_t)(2 * t + 1) * a.fsin + (size_t)col * H + k] : czero<R>();
-  }
-#pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int e = threadIdx.x + q * NT;
-    if (e < TOT) {
-      const int k = e % H;
-      const int t = (e / H) % 4;
-      const int cr = e / (4 * H);
-      zpack<R>(lines + (9 * (cr / 2) + 4 * (cr % 2) + t) * LP, M, k, lx[q], ly[q]);
-    }
-  }
-  for (int e = threadIdx.x; e < CP * H; e += NT) {
-    const int k = e % H, pr = e / H;
-    const int c0 = col0 + 2 * pr;
-    const C2<R> X = c0 < a.ncols ? a.in[(size_t)8 * a.fsin + (size_t)c0 * H + k] : czero<R>();
-    const C2<R> Y = c0 + 1 < a.ncols ? a.in[(size_t)8 * a.fsin + (size_t)(c0 + 1) * H + k] : czero<R>();
-    zpack<R>(lines + (9 * pr + 8) * LP, M, k, X, Y);
-  }
-  for (int e = threadIdx.x; e < NL * (N / 2 - 1); e += NT) {
-    const int l = e / (N / 2 - 1), p = H + e % (N / 2 - 1);
-    lines[l * LP + zi<R>(p)] = czero<R>();
-  }
-  __syncthreads();
-  fft_zlines<R, M, true, NT, NL>(lines, tw);
-  constexpr int QX = (CP * M + NT - 1) / NT;
-  C2<R> res[QX][6];
-#pragma unroll
-  for (int q = 0; q < QX; ++q) {
-    const int e = threadIdx.x + q * NT;
-    if (e < CP * M) {
-      const int pr = e / M, p = e % M;
-      const C2<R> Z = lines[(9 * pr + 8) * LP + zi<R>(p)];
-#pragma unroll
-      for (int cc = 0; cc < 2; ++cc) {
-        const C2<R>* L0 = lines + (9 * pr + 4 * cc) * LP;
-        const C2<R> A = L0[zi<R>(p)], B = L0[LP + zi<R>(p)], C = L0[2 * LP + zi<R>(p)], D = L0[3 * LP + zi<R>(p)];
-        const R ux = A.x, uy = A.y, uz = B.x, wx = B.y, wy = C.x, wz = C.y;
-        const R cx = D.x, cy = D.y, cz = cc == 0 ? Z.x : Z.y;
-        // a_bar = w x cb ; o_bar = cb x u
-        const R abx = wy * cz - wz * cy, aby = wz * cx - wx * cz, abz = wx * cy - wy * cx;
-        const R obx = cy * uz - cz * uy, oby = cz * ux - cx * uz, obz = cx * uy - cy * ux;
-        res[q][3 * cc + 0] = cmk<R>(abx, aby);
-        res[q][3 * cc + 1] = cmk<R>(abz, obx);
-        res[q][3 * cc + 2] = cmk<R>(oby, obz);
-      }
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < QX; ++q) {
-    const int e = threadIdx.x + q * NT;
-    if (e < CP * M) {
-      const int pr = e / M, p = e % M;
-#pragma unroll
-      for (int j = 0; j < 6; ++j) lines[(6 * pr + j) * LP + zi<R>(p)] = res[q][j];
-    }
-  }
-  __syncthreads();
-  fft_zlines<R, M, false, NT, 6 * CP>(lines, tw);
-  for (int e = threadIdx.x; e < CP * 6 * H; e += NT) {
-    const int k = e % H;
-    const int j = (e / H) % 6;
-    const int pr = e / (6 * H);
-    const int cc = j / 3, t = j % 3;
-    const int col = col0 + 2 * pr + cc;
+    const int t = (e / H) % 3;
+    const int c = e / (3 * H);
+    const int col = col0 + c;
     if (col >= a.ncols) continue;
     C2<R> X, Y;
-    zunpack<R>(lines + (6 * pr + j) * LP, M, k, X, Y);
+    zunpack<R>(B + (t * 2 * CP + c) * LP, M, k, X, Y);
     a.out[(size_t)(2 * t) * a.fsout + (size_t)col * H + k] = X;
     a.out[(size_t)(2 * t + 1) * a.fsout + (size_t)col * H + k] = Y;
   }

@@ -135,8 +135,13 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
   cudaError_t e;
   {
     TimerScope ts(p.timer, PASS_A1, s);
-    OpAdjXInv<R> o{8, H, N, M, (R)(1.0 / ((double)N * N * N)), (R)(1.0 / scale), ks,
-                   p.x, p.cs, p.nb, p.etd, p.slot, p.fac, p.dt, p.bufA, fsA1};
+    // c_bar source into bufB (free until A2 writes it)
+    CbarArgs<R> ca{N, H, (R)(1.0 / scale), ks, p.nb, p.cs, p.etd, p.slot, p.fac, p.dt, p.bufB};
+    const size_t nm = (size_t)N * N * H;
+    k_adj_cbar<R><<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(ca);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    OpAdjXInv<R> o{8, H, N, M, (R)(1.0 / ((double)N * N * N)), ks, p.x, p.cs, p.bufB, p.bufA, fsA1};
     e = launch_lines<R, M, true, true>(o, N, p.twM, s);
     if (e != cudaSuccess) return e;
   }
@@ -149,8 +154,8 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
   {
     TimerScope ts(p.timer, PASS_A3, s);
     constexpr int CP = zpairs<M, 384>();
-    constexpr int NT = zthreads<R, 9 * CP, M>();
-    const size_t smem = (size_t)9 * CP * zpad_len<R>(M) * sizeof(C2<R>);
+    constexpr int NT = adj_z_threads<R, M, CP>();
+    const size_t smem = (size_t)adj_z_smem_elems<R, M, CP>() * sizeof(C2<R>);
     constexpr auto kern = k_adj_z<R, M, CP, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;

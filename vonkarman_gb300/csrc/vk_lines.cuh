@@ -117,7 +117,7 @@ struct MapContig {
   static constexpr int elems() { return NLINES * zpad_len<R>(L); }
 };
 
-template <typename R, int L, bool INV, int NT, int NLINES, class MAP, int S, int NS>
+template <typename R, int L, bool INV, int NT, int NLINES, class MAP, int S, int NS, bool SL = false>
 struct RegStage {
   static constexpr int RAD = rradix<R, MAP::CONTIG>(L, S);
   static constexpr int NB = L / RAD;            // butterflies per line
@@ -174,7 +174,8 @@ struct RegStage {
       }
     }
     // a later stage writes the buffer it has just read: wait for all readers
-    if constexpr (S > 0 && !LAST) __syncthreads();
+    // (the last stage too when its outputs go back into the buffer, SL)
+    if constexpr (S > 0 && (!LAST || SL)) __syncthreads();
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int g = tid + q * NT;
@@ -200,7 +201,7 @@ struct RegStage {
     }
     if constexpr (!LAST) {
       __syncthreads();
-      RegStage<R, L, INV, NT, NLINES, MAP, S + 1, NS * RAD>::run(xb, tw, ld, pp, st);
+      RegStage<R, L, INV, NT, NLINES, MAP, S + 1, NS * RAD, SL>::run(xb, tw, ld, pp, st);
     }
   }
 };
@@ -208,12 +209,14 @@ struct RegStage {
 // Transform NLINES lines.  All NT threads must call it; the exchange buffer
 // xb (MAP::elems() elements) must not be in use by any thread.  Returns with
 // no synchronisation after the last stage.
-template <typename R, int L, bool INV, int NT, int NLINES, class MAP = MapInterleaved<R, L, NLINES>, class LD,
-          class PP, class ST>
+// SL: the store functor writes into xb itself (in place), so the last stage
+// also waits for all readers before storing.
+template <typename R, int L, bool INV, int NT, int NLINES, class MAP = MapInterleaved<R, L, NLINES>, bool SL = false,
+          class LD, class PP, class ST>
 __device__ __forceinline__ void fft_lines(C2<R>* xb, const C2<R>* __restrict__ tw, const LD& ld, const PP& pp,
                                           const ST& st) {
   static_assert(rstages<R>(L) > 0, "unsupported FFT length");
-  RegStage<R, L, INV, NT, NLINES, MAP, 0, 1>::run(xb, tw, ld, pp, st);
+  RegStage<R, L, INV, NT, NLINES, MAP, 0, 1, SL>::run(xb, tw, ld, pp, st);
 }
 // pp for inputs that need no arithmetic after the load
 struct PrepNone {

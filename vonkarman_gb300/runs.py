@@ -5,8 +5,15 @@ Tier-1 diagnostics, stop at the first step whose time reaches ``max_time``)
 with the diagnostics recorded on the device by ``vk_run`` and read back once
 per chunk instead of once per step.
 
-Two workloads are run from here (``python -m vonkarman_gb300.runs <name>``):
+Workloads run from here (``python -m vonkarman_gb300.runs <name>``):
 
+* ``tg``     -- Taylor-Green N=64, nu = 6.25e-4, fixed dt = 1e-3, 100 steps,
+  Tier-1 after every step, E(k) at step 100 (FP64): steps/s with the
+  diagnostics and device-timed steps/s without them.
+* ``isotropic`` -- random isotropic (von Karman kp = 4, E = 0.5, seed 42)
+  N=256, nu = 1e-3, adaptive CFL 0.5, to t = 2, Tier-1 after every step and
+  E(k) every 10 steps, FP64 and FP32-bulk: steps/s with the diagnostics, and
+  the FP32-bulk error against FP64 at t = 2.
 * ``tubes``  -- anti-parallel Lamb-Oseen tubes (circulation +-1, core radius
   0.25, separation 1.0 about (pi, pi), centre lines displaced in x by
   0.1 sin z), nu = 5e-4, adaptive CFL 0.5, to t = 5, Tier-1 after every step,
@@ -102,6 +109,65 @@ def tubes(n: int = 512, nu: float = 5e-4, t_end: float = 5.0, rate_steps: int = 
     return out
 
 
+def tg(n: int = 64, nu: float = 6.25e-4, dt: float = 1e-3, steps: int = 100, device: int = 0) -> dict:
+    from .solver import energy_spectrum
+
+    grid = GridSpec(n)
+    u0 = ics.taylor_green(n)
+    s = Periodic3D(grid, nu, u0, SolverOptions(dt_mode="fixed", dt_fixed=dt, device=device))
+    s.run(3, every=1)                     # warm-up (kernel set-up)
+    s.restore_state(u0, 0.0, 0, dt)
+    t0 = time.perf_counter()
+    recs = s.run(steps, every=1)
+    _, spec = energy_spectrum(s)
+    wall = time.perf_counter() - t0
+    s.restore_state(u0, 0.0, 0, dt)
+    rate = 1000.0 * steps / s.step_timed(steps)
+    last = recs[-1]
+    s.close()
+    return {"workload": f"Taylor-Green N={n}, nu={nu}, fixed dt={dt}, {steps} steps, Tier-1 every step, "
+                        f"E(k) at step {steps}, FP64",
+            "steps_per_s_with_diagnostics": steps / wall, "steps_per_s": rate,
+            "energy": last.energy, "enstrophy": last.enstrophy, "max_vorticity": last.max_vorticity,
+            "spectrum_sum": float(np.sum(spec))}
+
+
+def isotropic(n: int = 256, nu: float = 1e-3, t_end: float = 2.0, spectrum_every: int = 10,
+              device: int = 0) -> dict:
+    from .solver import energy_spectrum
+
+    grid = GridSpec(n)
+    u0 = ics.von_karman_isotropic(n, kp=4.0, energy=0.5, seed=42)
+    out = {"workload": f"random isotropic von Karman kp=4 E=0.5 seed 42, N={n}, nu={nu}, adaptive CFL 0.5, "
+                       f"to t={t_end}, Tier-1 every step, E(k) every {spectrum_every} steps", "forms": {}}
+    series, spectra = {}, {}
+    for prec in ("fp64", "fp32bulk"):
+        s = Periodic3D(grid, nu, u0, SolverOptions(precision=prec, device=device))
+        recs, specs = [], []
+        t0 = time.perf_counter()
+        while s.time() < t_end:
+            recs.extend(s.run(1, every=1))
+            if s.step_count() % spectrum_every == 0:
+                specs.append(energy_spectrum(s)[1])
+        wall = time.perf_counter() - t0
+        series[prec], spectra[prec] = recs, specs
+        out["forms"][prec] = {"steps": len(recs), "t_last": recs[-1].time, "wall_s": wall,
+                              "steps_per_s_with_diagnostics": len(recs) / wall,
+                              "energy_t_end": interp_at(recs, t_end, "energy"),
+                              "enstrophy_t_end": interp_at(recs, t_end, "enstrophy"),
+                              "max_vorticity_t_end": interp_at(recs, t_end, "max_vorticity")}
+        s.close()
+    f64, f32 = out["forms"]["fp64"], out["forms"]["fp32bulk"]
+    out["rel_error_at_t_end"] = {k: abs(f32[k + "_t_end"] - f64[k + "_t_end"]) / abs(f64[k + "_t_end"])
+                                 for k in ("energy", "enstrophy", "max_vorticity")}
+    k = min(len(spectra["fp64"]), len(spectra["fp32bulk"]))
+    if k:
+        a, b = spectra["fp64"][k - 1], spectra["fp32bulk"][k - 1]
+        keep = a > 1e-12 * a.max()
+        out["spectrum_max_rel_shell_last_common"] = float(np.max(np.abs(b - a)[keep] / a[keep]))
+    return out
+
+
 def _grad_rel(g, g_ref, n: int) -> float:
     d = [a - b for a, b in zip(g, g_ref)]
     return math.sqrt(l2_inner(d, d, n) / l2_inner(g_ref, g_ref, n))
@@ -147,15 +213,19 @@ def ascent(n: int = 256, nu: float = 2e-3, dt: float = 1e-3, nsteps: int = 1000,
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("workload", choices=["tubes", "ascent"])
+    ap.add_argument("workload", choices=["tg", "isotropic", "tubes", "ascent"])
     ap.add_argument("--n", type=int, default=None)
-    ap.add_argument("--t-end", type=float, default=5.0)
+    ap.add_argument("--t-end", type=float, default=None)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--iters", type=int, default=10)
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
-    if a.workload == "tubes":
-        r = tubes(n=a.n or 512, t_end=a.t_end, device=a.device)
+    if a.workload == "tg":
+        r = tg(n=a.n or 64, device=a.device)
+    elif a.workload == "isotropic":
+        r = isotropic(n=a.n or 256, t_end=a.t_end or 2.0, device=a.device)
+    elif a.workload == "tubes":
+        r = tubes(n=a.n or 512, t_end=a.t_end or 5.0, device=a.device)
     else:
         r = ascent(n=a.n or 256, nsteps=a.steps, iters=a.iters, device=a.device)
     print(json.dumps(r))

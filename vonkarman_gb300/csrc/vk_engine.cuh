@@ -216,14 +216,14 @@ inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
   NZArgs<R> a{N * N, p.bufB, fs, p.out, p.which};
   const int nb = (N * N + 2 * CP - 1) / (2 * CP);
   if (both) {
-    constexpr int NT = zthreads<R, 6 * CP, N>();
+    constexpr int NT = nz_threads<R, N, CP, true>();
     const size_t smem = (size_t)6 * CP * zpad_len<R>(N) * sizeof(C2<R>);
     constexpr auto kern = k_nz_max<R, N, CP, true, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
     kern<<<nb, NT, smem, s>>>(a, p.twN);
   } else {
-    constexpr int NT = zthreads<R, 3 * CP, N>();
+    constexpr int NT = nz_threads<R, N, CP, false>();
     const size_t smem = (size_t)3 * CP * zpad_len<R>(N) * sizeof(C2<R>);
     constexpr auto kern = k_nz_max<R, N, CP, false, NT>;
     e = prepare_kernel<kern>(smem);

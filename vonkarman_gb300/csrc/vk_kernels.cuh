@@ -400,101 +400,6 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long* p, double v) 
   atomicMax(p, (unsigned long long)__double_as_longlong(v));
 }
 
-template <typename R, int N, int CP, bool BOTH, int NT>
-__global__ void __launch_bounds__(NT, min_blocks<NT>()) k_nz_max(NZArgs<R> a, const C2<R>* __restrict__ tw) {
-  constexpr int H = N / 2 + 1;
-  constexpr int LPP = BOTH ? 6 : 3;   // lines per column pair
-  constexpr int NL = LPP * CP;
-  constexpr int LP = zpad_len<R>(N);
-  extern __shared__ __align__(16) unsigned char vk_smem[];
-  C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
-  __shared__ double red[2][32];
-  __shared__ int redn;
-  if (threadIdx.x == 0) redn = 0;
-  const int col0 = blockIdx.x * 2 * CP;
-  for (int e = threadIdx.x; e < 2 * CP * (LPP / 2) * H; e += NT) {
-    const int k = e % H;
-    const int t = (e / H) % (LPP / 2);
-    const int cr = e / ((LPP / 2) * H);
-    const int col = col0 + cr;
-    const int pr = cr / 2, cc = cr % 2;
-    C2<R> X = czero<R>(), Y = czero<R>();
-    if (BOTH) {
-      if (col < a.ncols) {
-        X = a.in[(size_t)(2 * t) * a.fs + (size_t)col * H + k];
-        Y = a.in[(size_t)(2 * t + 1) * a.fs + (size_t)col * H + k];
-      }
-      zpack<R>(lines + (6 * pr + 3 * cc + t) * LP, N, k, X, Y);
-    } else {
-      // t in {0}: each column loads its f0/f1 pair; the f2 fields of the two
-      // columns of a pair share one line.
-      if (col < a.ncols) {
-        X = a.in[(size_t)col * H + k];
-        Y = a.in[a.fs + (size_t)col * H + k];
-      }
-      zpack<R>(lines + (3 * pr + cc) * LP, N, k, X, Y);
-    }
-  }
-  if (!BOTH) {
-    for (int e = threadIdx.x; e < CP * H; e += NT) {
-      const int k = e % H, pr = e / H;
-      const int c0 = col0 + 2 * pr;
-      C2<R> X = czero<R>(), Y = czero<R>();
-      if (c0 < a.ncols) X = a.in[2 * a.fs + (size_t)c0 * H + k];
-      if (c0 + 1 < a.ncols) Y = a.in[2 * a.fs + (size_t)(c0 + 1) * H + k];
-      zpack<R>(lines + (3 * pr + 2) * LP, N, k, X, Y);
-    }
-  }
-  __syncthreads();
-  fft_zlines<R, N, true, NT, NL>(lines, tw);
-  double m1 = 0.0, m2 = 0.0;
-  int bad = 0;
-  for (int e = threadIdx.x; e < CP * N; e += NT) {
-    const int pr = e / N, p = e % N;
-#pragma unroll
-    for (int cc = 0; cc < 2; ++cc) {
-      if (col0 + 2 * pr + cc >= a.ncols) continue;
-      if (BOTH) {
-        const C2<R>* L0 = lines + (6 * pr + 3 * cc) * LP;
-        const C2<R> A = L0[zi<R>(p)], B = L0[LP + zi<R>(p)], C = L0[2 * LP + zi<R>(p)];
-        const double ux = A.x, uy = A.y, uz = B.x, wx = B.y, wy = C.x, wz = C.y;
-        const double s1 = ux * ux + uy * uy + uz * uz;
-        const double s2 = wx * wx + wy * wy + wz * wz;
-        bad |= (s1 != s1) | (s2 != s2);
-        m1 = fmax(m1, s1);
-        m2 = fmax(m2, s2);
-      } else {
-        const C2<R> A = lines[(3 * pr + cc) * LP + zi<R>(p)];
-        const C2<R> Z = lines[(3 * pr + 2) * LP + zi<R>(p)];
-        const double fx = A.x, fy = A.y, fz = cc == 0 ? Z.x : Z.y;
-        const double s = fx * fx + fy * fy + fz * fz;
-        bad |= (s != s);
-        m1 = fmax(m1, s);
-      }
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
-    m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
-  }
-  const int w = threadIdx.x / 32, ln = threadIdx.x % 32;
-  if (bad) atomicOr(&redn, 1);
-  if (ln == 0) { red[0][w] = m1; red[1][w] = m2; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double r1 = 0.0, r2 = 0.0;
-    for (int i = 0; i < NT / 32; ++i) { r1 = fmax(r1, red[0][i]); r2 = fmax(r2, red[1][i]); }
-    if (BOTH) {
-      atomic_max_pos(&a.out->umax2, r1);
-      atomic_max_pos(&a.out->wmax2, r2);
-    } else if (a.which == 2) {
-      atomic_max_pos(&a.out->wmax2, r1);
-    } else {
-      atomic_max_pos(&a.out->umax2, r1);
-    }
-    if (redn) atomicOr(&a.out->nan_flag, 1);
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Standalone backend z passes (FftBackend::r2c_3d / c2r_3d z stage,

@@ -147,6 +147,8 @@ struct RegStage {
         if (G % NT == 0 || g < G) {
           const int l = MAP::template line<NB>(g);
           const int j = MAP::template bfly<NB>(g);
+          __builtin_assume(j >= 0 && j < NB);
+          __builtin_assume(l >= 0 && l < NLINES);
 #pragma unroll
           for (int r0 = 0; r0 < RAD; r0 += CH) {
             Raw raw[CH];
@@ -168,6 +170,8 @@ struct RegStage {
         if (G % NT == 0 || g < G) {
           const int l = MAP::template line<NB>(g);
           const int j = MAP::template bfly<NB>(g);
+          __builtin_assume(j >= 0 && j < NB);
+          __builtin_assume(l >= 0 && l < NLINES);
 #pragma unroll
           for (int r = 0; r < RAD; ++r) v[q][r] = xb[MAP::template idx<S - 1>(j + r * NB, l)];
         }
@@ -182,6 +186,8 @@ struct RegStage {
       if (G % NT == 0 || g < G) {
         const int l = MAP::template line<NB>(g);
         const int j = MAP::template bfly<NB>(g);
+        __builtin_assume(j >= 0 && j < NB);
+        __builtin_assume(l >= 0 && l < NLINES);
         const int k = j % NS;
         C2<R> w[RAD];
         if constexpr (S > 0) {
@@ -458,5 +464,113 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
     }
   }
 }
+
+// ---------------------------------------------------------------------------
+// N-grid z pass on the register engine: c2r of u and/or omega (already x/y
+// inverted and scaled by 1/N^3) packed in pairs, and max |u|^2, max |omega|^2
+// over the N^3 grid (solver.rs:180-218 and :537-567).  Lines per column pair:
+// BOTH: l = 6 pr + 3 cc + t, the pair t of column cc; otherwise l = 3 pr + cc
+// (f0 + i f1 of column cc) and 3 pr + 2 (f2 of both columns).  The inverse
+// writes its physical values in place; the maxima follow.
+// ---------------------------------------------------------------------------
+template <typename R, int N, int CP, bool BOTH>
+__host__ __device__ constexpr int nz_threads() {
+  return cmin(rthreads<R, N, (BOTH ? 6 : 3) * CP, true>(), 384);
+}
+
+template <typename R, int N, int CP, bool BOTH, int NT>
+__global__ void __launch_bounds__(NT, N >= 512 ? 1 : cmax(1, (sizeof(R) == 8 ? 768 : 512) / NT))
+k_nz_max(NZArgs<R> a, const C2<R>* __restrict__ tw) {
+  constexpr int H = N / 2 + 1;
+  constexpr int LPP = BOTH ? 6 : 3;   // lines per column pair
+  constexpr int NL = LPP * CP;
+  constexpr int LP = zpad_len<R>(N);
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
+  __shared__ double red[2][32];
+  __shared__ int redn;
+  if (threadIdx.x == 0) redn = 0;
+  const int col0 = blockIdx.x * 2 * CP;
+  fft_lines<R, N, true, NT, NL, MapContig<R, N, NL>, true>(
+      lines, tw,
+      [&](int l, int p) -> C2x2<R> {
+        const int pr = l / LPP, j = l % LPP;
+        int fx, fy, cx, cy;
+        if (BOTH) {
+          const int cc = j / 3, t = j % 3;
+          fx = 2 * t; fy = 2 * t + 1;
+          cx = cy = col0 + 2 * pr + cc;
+        } else if (j < 2) {
+          fx = 0; fy = 1;
+          cx = cy = col0 + 2 * pr + j;
+        } else {
+          fx = fy = 2;
+          cx = col0 + 2 * pr;
+          cy = cx + 1;
+        }
+        const int k = p < H ? p : N - p;
+        C2x2<R> r{};
+        if (cx < a.ncols) r.a = a.in[(size_t)fx * a.fs + (size_t)cx * H + k];
+        if (cy < a.ncols) r.b = a.in[(size_t)fy * a.fs + (size_t)cy * H + k];
+        return r;
+      },
+      [&](int, int p, const C2x2<R>& r) -> C2<R> {   // Z = X + i Y with the Hermitian extension
+        const C2<R> X = r.a, Y = r.b;
+        if (p == 0 || 2 * p == N) return cmk<R>(X.x, Y.x);   // c2r drops these imaginary parts
+        return p < H ? cmk<R>(X.x - Y.y, X.y + Y.x) : cmk<R>(X.x + Y.y, Y.x - X.y);
+      },
+      [&](int l, int p, C2<R> v) { lines[l * LP + zi<R>(p)] = v; });
+  __syncthreads();
+  // maxima in the working precision (the FP32-bulk form keeps FP64 only for
+  // the dt arithmetic that consumes them)
+  R m1 = R(0), m2 = R(0);
+  int bad = 0;
+  for (int e = threadIdx.x; e < CP * N; e += NT) {
+    const int pr = e / N, p = e % N;
+#pragma unroll
+    for (int cc = 0; cc < 2; ++cc) {
+      if (col0 + 2 * pr + cc >= a.ncols) continue;
+      if (BOTH) {
+        const C2<R>* L0 = lines + (6 * pr + 3 * cc) * LP;
+        const C2<R> A = L0[zi<R>(p)], B = L0[LP + zi<R>(p)], C = L0[2 * LP + zi<R>(p)];
+        const R ux = A.x, uy = A.y, uz = B.x, wx = B.y, wy = C.x, wz = C.y;
+        const R s1 = ux * ux + uy * uy + uz * uz;
+        const R s2 = wx * wx + wy * wy + wz * wz;
+        bad |= (s1 != s1) | (s2 != s2);
+        m1 = fmax(m1, s1);
+        m2 = fmax(m2, s2);
+      } else {
+        const C2<R> A = lines[(3 * pr + cc) * LP + zi<R>(p)];
+        const C2<R> Z = lines[(3 * pr + 2) * LP + zi<R>(p)];
+        const R fx = A.x, fy = A.y, fz = cc == 0 ? Z.x : Z.y;
+        const R s = fx * fx + fy * fy + fz * fz;
+        bad |= (s != s);
+        m1 = fmax(m1, s);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+  }
+  const int w = threadIdx.x / 32, ln = threadIdx.x % 32;
+  if (bad) atomicOr(&redn, 1);
+  if (ln == 0) { red[0][w] = (double)m1; red[1][w] = (double)m2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r1 = 0.0, r2 = 0.0;
+    for (int i = 0; i < NT / 32; ++i) { r1 = fmax(r1, red[0][i]); r2 = fmax(r2, red[1][i]); }
+    if (BOTH) {
+      atomic_max_pos(&a.out->umax2, r1);
+      atomic_max_pos(&a.out->wmax2, r2);
+    } else if (a.which == 2) {
+      atomic_max_pos(&a.out->wmax2, r1);
+    } else {
+      atomic_max_pos(&a.out->umax2, r1);
+    }
+    if (redn) atomicOr(&a.out->nan_flag, 1);
+  }
+}
+
 
 }  // namespace vk

@@ -111,6 +111,25 @@ def test_fp32bulk_gradient_vs_fp64(vk):
     assert nrel(grads[1], grads[0]) < 1e-4
 
 
+@pytest.mark.parametrize("n", [256, 512])
+def test_fp32bulk_gradient_vs_fp64_large_grids(vk, n):
+    # the 384- and 768-point plans of the adjoint chain (A1..A5), both forms
+    # against each other (the oracle is too slow at these sizes)
+    from vonkarman_gb300 import ics
+
+    nu, dt, nsteps = 2e-3, 1e-3, 2
+    u0 = ics.project_control(ics.von_karman_isotropic(n, kp=3.0, energy=0.5, seed=7), n)
+    out = []
+    for prec in ("fp64", "fp32bulk"):
+        s = vk.Periodic3D(vk.GridSpec(n), nu, u0, vk.SolverOptions(precision=prec, dt_mode="fixed", dt_fixed=dt))
+        J = s.adjoint_forward(nsteps, 1)
+        out.append((J, s.adjoint_backward()))
+        s.close()
+    (j64, g64), (j32, g32) = out
+    assert abs(j32 - j64) <= 1e-5 * abs(j64)
+    assert nrel(g32, g64) < 1e-4
+
+
 def test_adjoint_rejects_cfl_mode(vk):
     from vonkarman_gb300._native import VkError
 

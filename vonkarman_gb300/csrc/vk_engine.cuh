@@ -32,16 +32,16 @@ inline cudaError_t prepare_kernel(size_t smem) {
 
 // Register-resident strided pass (k_lines): nouter * hz lines per field in
 // tiles of NLINES.
-// Lines per CTA: 8 (row segments of 64 bytes in FP32, 128 in FP64).  X passes
-// (FFT axis = slowest array dimension) are marked so that the tile can differ
-// from the y passes; 16-line FP32 x tiles measured no faster.
-template <typename R, int L, bool XAXIS> struct NLof {
-  static constexpr int value = 8;
+// Lines per CTA: 8 (row segments of 64 bytes in FP32, 128 in FP64), and 16
+// for FP32 y passes without staged inputs (P4, NY: measured 6 % faster; the
+// staged P2 and the x passes measured slower with 16).
+template <typename R, int L, bool XAXIS, bool STAGED> struct NLof {
+  static constexpr int value = (!XAXIS && !STAGED && sizeof(R) == 4 && L <= 512) ? 16 : 8;
 };
 
 template <typename R, int L, bool INV, bool XAXIS = false, class Op>
 inline cudaError_t launch_lines(const Op& op, int nouter, const C2<R>* tw, cudaStream_t s) {
-  constexpr int NLINES = NLof<R, L, XAXIS>::value;
+  constexpr int NLINES = NLof<R, L, XAXIS, Op::STAGED_ANY>::value;
   constexpr int NT = cmin(rthreads<R, L, NLINES>(), 384);
   const size_t smem = lines_smem_bytes<R, L, NLINES>(op);
   constexpr auto kern = k_lines<R, L, INV, NLINES, NT, Op>;

@@ -89,7 +89,7 @@ __host__ __device__ constexpr int lines_min_blocks() {
   if constexpr (sizeof(R) == 8) {
     return L >= 512 ? 1 : cmax(1, 768 / NT);
   } else {
-    return L >= 768 ? (EPI ? 1 : 2) : EPI ? cmax(1, 512 / NT) : L >= 512 ? 2 : L >= 384 ? 3
+    return L >= 768 ? (EPI ? 1 : 2) : EPI ? cmax(1, 512 / NT) : L >= 512 ? 2 : L >= 384 ? (NT >= 384 ? 2 : 3)
          : NT < 128 ? 4 : cmax(1, 768 / NT);
   }
 }
@@ -229,6 +229,15 @@ struct PrepNone {
   template <class T> __device__ __forceinline__ T operator()(int, int, const T& v) const { return v; }
 };
 
+// Copy of the twiddle table in shared memory: the stages read it through the
+// shared-memory pipe instead of the L1/texture path, which the global loads
+// and stores of the passes keep busy.  No barrier is needed before the FFT:
+// the first stage reads no twiddles and ends with one.
+template <typename R, int L, int NT>
+__device__ __forceinline__ void load_twiddles(C2<R>* tw_s, const C2<R>* __restrict__ tw) {
+  for (int i = threadIdx.x; i < L; i += NT) tw_s[i] = tw[i];
+}
+
 // Generic strided pass: NLINES consecutive lines lam = outer * hz + z of one
 // field per CTA (blockIdx.x = f + nfields * tile), so no z tile is partly
 // empty.  Op supplies kind(f) in [0, NKIND) (fields of one kind share their
@@ -241,6 +250,12 @@ template <typename R, int L, bool INV, int NLINES, int NT, class Op>
 __global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op op, const C2<R>* __restrict__ tw, int nlines) {
   static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
   extern __shared__ __align__(16) unsigned char vk_smem[];
+  // ops that stage inputs through shared memory keep their twiddles in the
+  // global table (measured faster: their shared-memory pipe is the busier one)
+  constexpr bool TWS = !Op::STAGED_ANY;
+  __shared__ C2<R> tw_sm[TWS ? L : 1];
+  if constexpr (TWS) load_twiddles<R, L, NT>(tw_sm, tw);
+  const C2<R>* tw_s = TWS ? tw_sm : tw;
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   const int f = blockIdx.x % op.nfields;
   const int tile = blockIdx.x / op.nfields;
@@ -278,10 +293,10 @@ __global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op o
       }
       __syncthreads();
       fft_lines<R, L, INV, NT, NLINES>(
-          xb, tw, [&](int ll, int p) { return sin[p * NLINES + ll]; }, PrepNone{}, st);
+          xb, tw_s, [&](int ll, int p) { return sin[p * NLINES + ll]; }, PrepNone{}, st);
     } else {
       fft_lines<R, L, INV, NT, NLINES>(
-          xb, tw, [&](int, int p) { return op.template load<K>(f, outer, z, p); },
+          xb, tw_s, [&](int, int p) { return op.template load<K>(f, outer, z, p); },
           [&](int, int p, const auto& raw) { return op.template prep<K>(f, outer, z, p, raw); }, st);
     }
   });
@@ -325,6 +340,8 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int N = 2 * L / 3;
   static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
   extern __shared__ __align__(16) unsigned char vk_smem[];
+  __shared__ C2<R> tw_s[L];
+  load_twiddles<R, L, NT>(tw_s, tw);
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   C2<R>* keep = xb + rsmem_elems<R, L, NLINES>();   // 3 fields x N x NLINES
   const int H = a.H;
@@ -338,7 +355,7 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
       if (C > 0) __syncthreads();   // xb is reused
       const C2<R>* src = a.in + (size_t)C * a.fsin + (size_t)iy * H + z;
       fft_lines<R, L, false, NT, NLINES>(
-          xb, tw, [&](int, int p) { return src[(size_t)p * N * H]; }, PrepNone{},
+          xb, tw_s, [&](int, int p) { return src[(size_t)p * N * H]; }, PrepNone{},
           [&](int, int p, C2<R> v) {
             const int ix = unpad_pos(p, N, L);
             if (ix >= 0) keep[(C * N + ix) * NLINES + (int)(threadIdx.x % NLINES)] = v;
@@ -395,11 +412,13 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int LP = zpad_len<R>(M);
   constexpr int NI = 6 * CP, NF = 3 * CP;
   extern __shared__ __align__(16) unsigned char vk_smem[];
+  __shared__ C2<R> tw_s[M];
+  load_twiddles<R, M, NT>(tw_s, tw);
   C2<R>* A = reinterpret_cast<C2<R>*>(vk_smem);
   C2<R>* B = A + NI * LP;
   const int col0 = blockIdx.x * 2 * CP;
   fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>>(
-      A, tw,
+      A, tw_s,
       [&](int l, int p) -> C2x2<R> {
         const int t = l / (2 * CP);
         const int col = col0 + l % (2 * CP);
@@ -438,7 +457,7 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
   }
   __syncthreads();
   fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>>(
-      B, tw, [&](int l, int p) { return A[l * LP + zi<R>(p)]; }, PrepNone{},
+      B, tw_s, [&](int l, int p) { return A[l * LP + zi<R>(p)]; }, PrepNone{},
       [&](int l, int p, C2<R> v) { A[l * LP + zi<R>(p)] = v; });
   __syncthreads();
   for (int e = threadIdx.x; e < CP * 3 * H; e += NT) {
@@ -487,12 +506,14 @@ k_nz_max(NZArgs<R> a, const C2<R>* __restrict__ tw) {
   constexpr int LP = zpad_len<R>(N);
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
+  __shared__ C2<R> tw_s[N];
   __shared__ double red[2][32];
   __shared__ int redn;
+  load_twiddles<R, N, NT>(tw_s, tw);
   if (threadIdx.x == 0) redn = 0;
   const int col0 = blockIdx.x * 2 * CP;
   fft_lines<R, N, true, NT, NL, MapContig<R, N, NL>, true>(
-      lines, tw,
+      lines, tw_s,
       [&](int l, int p) -> C2x2<R> {
         const int pr = l / LPP, j = l % LPP;
         int fx, fy, cx, cy;

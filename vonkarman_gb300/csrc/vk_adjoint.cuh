@@ -171,12 +171,12 @@ k_adj_z(A3Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int LP = zpad_len<R>(M);
   constexpr int NI = 9 * CP, NF = 6 * CP;
   extern __shared__ __align__(16) unsigned char vk_smem[];
-  __shared__ C2<R> tw_s[M];
-  load_twiddles<R, M, NT>(tw_s, tw);
+  __shared__ C2<R> tw_s[twtab_elems<R, true>(M)];
+  load_twtab<R, M, true, NT>(tw_s, tw);
   C2<R>* A = reinterpret_cast<C2<R>*>(vk_smem);   // NI lines
   C2<R>* B = A + NI * LP;                          // NF lines
   const int col0 = blockIdx.x * 2 * CP;
-  fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>, true>(
+  fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>, true, true>(
       A, tw_s,
       [&](int l, int p) -> C2x2<R> {
         int fx, fy, cx, cy;
@@ -225,7 +225,7 @@ k_adj_z(A3Args<R> a, const C2<R>* __restrict__ tw) {
     }
   }
   __syncthreads();
-  fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>>(
+  fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>, false, true>(
       A, tw_s, [&](int l, int p) { return B[l * LP + zi<R>(p)]; }, PrepNone{},
       [&](int l, int p, C2<R> v) { B[l * LP + zi<R>(p)] = v; });
   __syncthreads();
@@ -349,8 +349,8 @@ k_adj_p5(A5Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int N = 2 * L / 3;
   static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
   extern __shared__ __align__(16) unsigned char vk_smem[];
-  __shared__ C2<R> tw_s[L];
-  load_twiddles<R, L, NT>(tw_s, tw);
+  __shared__ C2<R> tw_s[twtab_elems<R, false>(L)];
+  load_twtab<R, L, false, NT>(tw_s, tw);
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   C2<R>* acc = xb + rsmem_elems<R, L, NLINES>();   // 3 components x N x NLINES
   const int H = a.H;
@@ -367,7 +367,7 @@ k_adj_p5(A5Args<R> a, const C2<R>* __restrict__ tw) {
       constexpr int C = decltype(cc)::value;
       if (C > 0) __syncthreads();   // xb is reused
       const C2<R>* src = a.in + (size_t)C * a.fsin + (size_t)iy * H + z;
-      fft_lines<R, L, false, NT, NLINES>(
+      fft_lines<R, L, false, NT, NLINES, MapInterleaved<R, L, NLINES>, false, true>(
           xb, tw_s, [&](int, int p) { return src[(size_t)p * N * H]; }, PrepNone{},
           [&](int, int p, C2<R> v) {
             const int ix = unpad_pos(p, N, L);

@@ -62,6 +62,27 @@ __host__ __device__ constexpr int rthreads() {
     return cmax(round32(L / rradix<R, CONTIG>(L, S) * NLINES), rthreads<R, L, NLINES, CONTIG, S + 1>());
   }
 }
+// Per-stage twiddle tables (shared memory): stage S >= 1 of a plan reads
+// W_L^(r k TWS) for r = 1..RAD-1, k = 0..NS-1 at (r-1) NS + k, so that lanes
+// with consecutive k read consecutive entries (no bank conflicts) and lanes
+// with the same k read the same entry.
+template <typename R, bool CONTIG>
+__host__ __device__ constexpr int stage_ns(int L, int S) {
+  int ns = 1;
+  for (int s = 0; s < S; ++s) ns *= rradix<R, CONTIG>(L, s);
+  return ns;
+}
+template <typename R, bool CONTIG>
+__host__ __device__ constexpr int twtab_off(int L, int S) {
+  int off = 0;
+  for (int s = 1; s < S; ++s) off += (rradix<R, CONTIG>(L, s) - 1) * stage_ns<R, CONTIG>(L, s);
+  return off;
+}
+template <typename R, bool CONTIG>
+__host__ __device__ constexpr int twtab_elems(int L) {
+  return cmax(1, twtab_off<R, CONTIG>(L, rstages<R, CONTIG>(L)));
+}
+
 // FP32 with 8 lines: the first stage writes at stride RAD0 positions, so a
 // padding slot after every RAD0 positions spreads a warp over both halves of
 // the 32 banks.  FP64 rows of 8 lines are already 128 bytes.
@@ -117,7 +138,7 @@ struct MapContig {
   static constexpr int elems() { return NLINES * zpad_len<R>(L); }
 };
 
-template <typename R, int L, bool INV, int NT, int NLINES, class MAP, int S, int NS, bool SL = false>
+template <typename R, int L, bool INV, int NT, int NLINES, class MAP, int S, int NS, bool SL = false, bool TT = false>
 struct RegStage {
   static constexpr int RAD = rradix<R, MAP::CONTIG>(L, S);
   static constexpr int NB = L / RAD;            // butterflies per line
@@ -192,7 +213,13 @@ struct RegStage {
         C2<R> w[RAD];
         if constexpr (S > 0) {
 #pragma unroll
-          for (int r = 1; r < RAD; ++r) w[r] = tw[r * k * TWS];
+          for (int r = 1; r < RAD; ++r) {
+            if constexpr (TT) {
+              w[r] = tw[twtab_off<R, MAP::CONTIG>(L, S) + (r - 1) * NS + k];
+            } else {
+              w[r] = tw[r * k * TWS];
+            }
+          }
         }
         dft<R, INV, RAD, (S > 0)>(v[q], w);
         const int base = (j - k) * RAD + k;
@@ -207,7 +234,7 @@ struct RegStage {
     }
     if constexpr (!LAST) {
       __syncthreads();
-      RegStage<R, L, INV, NT, NLINES, MAP, S + 1, NS * RAD, SL>::run(xb, tw, ld, pp, st);
+      RegStage<R, L, INV, NT, NLINES, MAP, S + 1, NS * RAD, SL, TT>::run(xb, tw, ld, pp, st);
     }
   }
 };
@@ -216,26 +243,36 @@ struct RegStage {
 // xb (MAP::elems() elements) must not be in use by any thread.  Returns with
 // no synchronisation after the last stage.
 // SL: the store functor writes into xb itself (in place), so the last stage
-// also waits for all readers before storing.
+// also waits for all readers before storing.  TT: tw is the per-stage table
+// of load_twtab (shared memory), else the plain W_L^m table.
 template <typename R, int L, bool INV, int NT, int NLINES, class MAP = MapInterleaved<R, L, NLINES>, bool SL = false,
-          class LD, class PP, class ST>
+          bool TT = false, class LD, class PP, class ST>
 __device__ __forceinline__ void fft_lines(C2<R>* xb, const C2<R>* __restrict__ tw, const LD& ld, const PP& pp,
                                           const ST& st) {
   static_assert(rstages<R>(L) > 0, "unsupported FFT length");
-  RegStage<R, L, INV, NT, NLINES, MAP, 0, 1, SL>::run(xb, tw, ld, pp, st);
+  RegStage<R, L, INV, NT, NLINES, MAP, 0, 1, SL, TT>::run(xb, tw, ld, pp, st);
 }
 // pp for inputs that need no arithmetic after the load
 struct PrepNone {
   template <class T> __device__ __forceinline__ T operator()(int, int, const T& v) const { return v; }
 };
 
-// Copy of the twiddle table in shared memory: the stages read it through the
+// Per-stage twiddle tables in shared memory: the stages read them through the
 // shared-memory pipe instead of the L1/texture path, which the global loads
-// and stores of the passes keep busy.  No barrier is needed before the FFT:
-// the first stage reads no twiddles and ends with one.
-template <typename R, int L, int NT>
-__device__ __forceinline__ void load_twiddles(C2<R>* tw_s, const C2<R>* __restrict__ tw) {
-  for (int i = threadIdx.x; i < L; i += NT) tw_s[i] = tw[i];
+// and stores of the passes keep busy, and without bank conflicts.  No barrier
+// is needed before the FFT: the first stage reads no twiddles and ends with
+// one.
+template <typename R, int L, bool CONTIG, int NT>
+__device__ __forceinline__ void load_twtab(C2<R>* tab, const C2<R>* __restrict__ tw) {
+  constexpr int ST = rstages<R, CONTIG>(L);
+  for (int S = 1; S < ST; ++S) {
+    const int rad = rradix<R, CONTIG>(L, S), ns = stage_ns<R, CONTIG>(L, S);
+    const int tws = L / (ns * rad), off = twtab_off<R, CONTIG>(L, S);
+    for (int i = threadIdx.x; i < (rad - 1) * ns; i += NT) {
+      const int r = i / ns + 1, k = i - (r - 1) * ns;
+      tab[off + i] = tw[r * k * tws];
+    }
+  }
 }
 
 // Generic strided pass: NLINES consecutive lines lam = outer * hz + z of one
@@ -253,8 +290,8 @@ __global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op o
   // ops that stage inputs through shared memory keep their twiddles in the
   // global table (measured faster: their shared-memory pipe is the busier one)
   constexpr bool TWS = !Op::STAGED_ANY;
-  __shared__ C2<R> tw_sm[TWS ? L : 1];
-  if constexpr (TWS) load_twiddles<R, L, NT>(tw_sm, tw);
+  __shared__ C2<R> tw_sm[TWS ? twtab_elems<R, false>(L) : 1];
+  if constexpr (TWS) load_twtab<R, L, false, NT>(tw_sm, tw);
   const C2<R>* tw_s = TWS ? tw_sm : tw;
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   const int f = blockIdx.x % op.nfields;
@@ -292,10 +329,10 @@ __global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op o
         if (p < L) sin[p * NLINES + l] = op.template prep<K>(f, outer, z, p, raw[i]);
       }
       __syncthreads();
-      fft_lines<R, L, INV, NT, NLINES>(
+      fft_lines<R, L, INV, NT, NLINES, MapInterleaved<R, L, NLINES>, false, TWS>(
           xb, tw_s, [&](int ll, int p) { return sin[p * NLINES + ll]; }, PrepNone{}, st);
     } else {
-      fft_lines<R, L, INV, NT, NLINES>(
+      fft_lines<R, L, INV, NT, NLINES, MapInterleaved<R, L, NLINES>, false, TWS>(
           xb, tw_s, [&](int, int p) { return op.template load<K>(f, outer, z, p); },
           [&](int, int p, const auto& raw) { return op.template prep<K>(f, outer, z, p, raw); }, st);
     }
@@ -340,8 +377,8 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int N = 2 * L / 3;
   static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
   extern __shared__ __align__(16) unsigned char vk_smem[];
-  __shared__ C2<R> tw_s[L];
-  load_twiddles<R, L, NT>(tw_s, tw);
+  __shared__ C2<R> tw_s[twtab_elems<R, false>(L)];
+  load_twtab<R, L, false, NT>(tw_s, tw);
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   C2<R>* keep = xb + rsmem_elems<R, L, NLINES>();   // 3 fields x N x NLINES
   const int H = a.H;
@@ -354,7 +391,7 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
       constexpr int C = decltype(cc)::value;
       if (C > 0) __syncthreads();   // xb is reused
       const C2<R>* src = a.in + (size_t)C * a.fsin + (size_t)iy * H + z;
-      fft_lines<R, L, false, NT, NLINES>(
+      fft_lines<R, L, false, NT, NLINES, MapInterleaved<R, L, NLINES>, false, true>(
           xb, tw_s, [&](int, int p) { return src[(size_t)p * N * H]; }, PrepNone{},
           [&](int, int p, C2<R> v) {
             const int ix = unpad_pos(p, N, L);
@@ -412,12 +449,12 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int LP = zpad_len<R>(M);
   constexpr int NI = 6 * CP, NF = 3 * CP;
   extern __shared__ __align__(16) unsigned char vk_smem[];
-  __shared__ C2<R> tw_s[M];
-  load_twiddles<R, M, NT>(tw_s, tw);
+  __shared__ C2<R> tw_s[twtab_elems<R, true>(M)];
+  load_twtab<R, M, true, NT>(tw_s, tw);
   C2<R>* A = reinterpret_cast<C2<R>*>(vk_smem);
   C2<R>* B = A + NI * LP;
   const int col0 = blockIdx.x * 2 * CP;
-  fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>>(
+  fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>, false, true>(
       A, tw_s,
       [&](int l, int p) -> C2x2<R> {
         const int t = l / (2 * CP);
@@ -456,7 +493,7 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
     A[(2 * CP + pr) * LP + zp] = cmk<R>(c[1][0], c[1][1]);
   }
   __syncthreads();
-  fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>>(
+  fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>, false, true>(
       B, tw_s, [&](int l, int p) { return A[l * LP + zi<R>(p)]; }, PrepNone{},
       [&](int l, int p, C2<R> v) { A[l * LP + zi<R>(p)] = v; });
   __syncthreads();
@@ -506,13 +543,13 @@ k_nz_max(NZArgs<R> a, const C2<R>* __restrict__ tw) {
   constexpr int LP = zpad_len<R>(N);
   extern __shared__ __align__(16) unsigned char vk_smem[];
   C2<R>* lines = reinterpret_cast<C2<R>*>(vk_smem);
-  __shared__ C2<R> tw_s[N];
+  __shared__ C2<R> tw_s[twtab_elems<R, true>(N)];
   __shared__ double red[2][32];
   __shared__ int redn;
-  load_twiddles<R, N, NT>(tw_s, tw);
+  load_twtab<R, N, true, NT>(tw_s, tw);
   if (threadIdx.x == 0) redn = 0;
   const int col0 = blockIdx.x * 2 * CP;
-  fft_lines<R, N, true, NT, NL, MapContig<R, N, NL>, true>(
+  fft_lines<R, N, true, NT, NL, MapContig<R, N, NL>, true, true>(
       lines, tw_s,
       [&](int l, int p) -> C2x2<R> {
         const int pr = l / LPP, j = l % LPP;

@@ -203,140 +203,188 @@ __device__ __forceinline__ C2<R> axpby(R a, C2<R> x, R b, C2<R> y) {
   return cmk<R>(a * x.x + b * y.x, a * x.y + b * y.y);
 }
 
-// The inputs of all three components are loaded before any result is
-// stored: a store may alias a later load as far as the compiler knows, so
-// interleaving them would serialise the loads.
-template <typename R>
-__device__ __forceinline__ void stage_apply(const StageArgs<R>& s, size_t idx, int m, R k2, const C2<R>* nl) {
+// Stage epilogue of NM modes at once: the inputs of all modes and all three
+// components are loaded before any result is stored (a store may alias a
+// later load as far as the compiler knows, so interleaving them would
+// serialise the loads).  ok[q] = false skips mode q.
+template <typename R, int NM>
+__device__ __forceinline__ void stage_apply_n(const StageArgs<R>& s, const size_t* idx, const int* m, const R* k2,
+                                              const C2<R> (*nl)[3], const bool* ok) {
   const size_t cs = s.cs;
   if (s.op == ST_NL_OUT) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) s.out[c * cs + idx] = nl[c];
+    for (int q = 0; q < NM; ++q) {
+      if (!ok[q]) continue;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) s.out[c * cs + idx[q]] = nl[q][c];
+    }
     return;
   }
   const double dt = *s.dt;
-  C2<R> u[3];
+  C2<R> u[NM][3];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) u[c] = s.u[c * cs + idx];
+  for (int q = 0; q < NM; ++q) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) u[q][c] = ok[q] ? s.u[c * cs + idx[q]] : czero<R>();
+  }
   if (s.op >= ST_RK4_1) {
     // rhs = N + (-nu k^2) state  (rk4.rs:30-45)
-    const R visc = (R)(-s.nu) * k2;
     const R half = (R)(0.5 * dt);
-    C2<R> st[3], a[3];
+    C2<R> st[NM][3], a[NM][3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      st[c] = s.op == ST_RK4_1 ? u[c] : s.temp[c * cs + idx];
-      a[c] = s.op == ST_RK4_1 ? czero<R>() : s.acc[c * cs + idx];
+    for (int q = 0; q < NM; ++q) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const bool rd = ok[q] && s.op != ST_RK4_1;
+        st[q][c] = rd ? s.temp[c * cs + idx[q]] : u[q][c];
+        a[q][c] = rd ? s.acc[c * cs + idx[q]] : czero<R>();
+      }
     }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const size_t i = c * cs + idx;
-      const C2<R> rhs = cmk<R>(nl[c].x + visc * st[c].x, nl[c].y + visc * st[c].y);
-      if (s.op == ST_RK4_1) {
-        s.acc[i] = rhs;
-        s.temp[i] = cmk<R>(u[c].x + half * rhs.x, u[c].y + half * rhs.y);
-      } else if (s.op == ST_RK4_2 || s.op == ST_RK4_3) {
-        s.acc[i] = cmk<R>(a[c].x + R(2) * rhs.x, a[c].y + R(2) * rhs.y);
-        const R h = s.op == ST_RK4_2 ? half : (R)dt;
-        s.temp[i] = cmk<R>(u[c].x + h * rhs.x, u[c].y + h * rhs.y);
-      } else {
-        const R sixth = (R)(dt / 6.0);
-        s.u[i] = cmk<R>(u[c].x + sixth * (a[c].x + rhs.x), u[c].y + sixth * (a[c].y + rhs.y));
+    for (int q = 0; q < NM; ++q) {
+      if (!ok[q]) continue;
+      const R visc = (R)(-s.nu) * k2[q];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const size_t i = c * cs + idx[q];
+        const C2<R> rhs = cmk<R>(nl[q][c].x + visc * st[q][c].x, nl[q][c].y + visc * st[q][c].y);
+        if (s.op == ST_RK4_1) {
+          s.acc[i] = rhs;
+          s.temp[i] = cmk<R>(u[q][c].x + half * rhs.x, u[q][c].y + half * rhs.y);
+        } else if (s.op == ST_RK4_2 || s.op == ST_RK4_3) {
+          s.acc[i] = cmk<R>(a[q][c].x + R(2) * rhs.x, a[q][c].y + R(2) * rhs.y);
+          const R h = s.op == ST_RK4_2 ? half : (R)dt;
+          s.temp[i] = cmk<R>(u[q][c].x + h * rhs.x, u[q][c].y + h * rhs.y);
+        } else {
+          const R sixth = (R)(dt / 6.0);
+          s.u[i] = cmk<R>(u[q][c].x + sixth * (a[q][c].x + rhs.x), u[q][c].y + sixth * (a[q][c].y + rhs.y));
+        }
       }
     }
     return;
   }
-  const double* e = s.etd + (size_t)m * ETD_STRIDE;
-  switch (s.op) {
-    case ST_ETD_REF_1: {  // solver.rs:264-281
-      const R eh = (R)e[E_HALF], q = (R)(dt * e[E_A21]);
+  // ETD coefficients of each mode (table keyed by the |k|^2 index)
+  const double* e[NM];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        s.n1[c * cs + idx] = nl[c];
-        s.temp[c * cs + idx] = axpby<R>(eh, u[c], q, nl[c]);
+  for (int q = 0; q < NM; ++q) e[q] = s.etd + (size_t)(ok[q] ? m[q] : 0) * ETD_STRIDE;
+  switch (s.op) {
+    case ST_ETD_REF_1:    // solver.rs:264-281
+    case ST_ETD_CM_1: {   // textbook: a = E2 u + (h/2) phi1(z/2) N1
+      const double f = s.op == ST_ETD_REF_1 ? dt : 0.5 * dt;
+      R eh[NM], qq[NM];
+#pragma unroll
+      for (int q = 0; q < NM; ++q) { eh[q] = (R)e[q][E_HALF]; qq[q] = (R)(f * e[q][E_A21]); }
+#pragma unroll
+      for (int q = 0; q < NM; ++q) {
+        if (!ok[q]) continue;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          s.n1[c * cs + idx[q]] = nl[q][c];
+          s.temp[c * cs + idx[q]] = axpby<R>(eh[q], u[q][c], qq[q], nl[q][c]);
+        }
       }
       break;
     }
-    case ST_ETD_REF_2: {  // solver.rs:291-308; acc starts the final sum
-      const R b1 = (R)e[E_B1], b23 = (R)e[E_B23], eh = (R)e[E_HALF], q = (R)(dt * e[E_A21]);
-      C2<R> n1[3];
+    case ST_ETD_REF_2:    // solver.rs:291-308; acc starts the final sum
+    case ST_ETD_CM_2: {   // b = E2 u + (h/2) phi1(z/2) N2
+      const double f = s.op == ST_ETD_REF_2 ? dt : 0.5 * dt;
+      R b1[NM], b23[NM], eh[NM], qq[NM];
+      C2<R> n1[NM][3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) n1[c] = s.n1[c * cs + idx];
+      for (int q = 0; q < NM; ++q) {
+        b1[q] = (R)e[q][E_B1]; b23[q] = (R)e[q][E_B23]; eh[q] = (R)e[q][E_HALF]; qq[q] = (R)(f * e[q][E_A21]);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        s.acc[c * cs + idx] = axpby<R>(b1, n1[c], b23, nl[c]);
-        s.temp[c * cs + idx] = axpby<R>(eh, u[c], q, nl[c]);
+        for (int c = 0; c < 3; ++c) n1[q][c] = ok[q] ? s.n1[c * cs + idx[q]] : czero<R>();
+      }
+#pragma unroll
+      for (int q = 0; q < NM; ++q) {
+        if (!ok[q]) continue;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          s.acc[c * cs + idx[q]] = axpby<R>(b1[q], n1[q][c], b23[q], nl[q][c]);
+          s.temp[c * cs + idx[q]] = axpby<R>(eh[q], u[q][c], qq[q], nl[q][c]);
+        }
       }
       break;
     }
     case ST_ETD_REF_3: {  // solver.rs:318-344
-      const R b23 = (R)e[E_B23], ef = (R)e[E_FULL], q = (R)(dt * e[E_A41]);
-      C2<R> n1[3], a[3];
+      R b23[NM], ef[NM], qq[NM];
+      C2<R> n1[NM][3], a[NM][3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        n1[c] = s.n1[c * cs + idx];
-        a[c] = s.acc[c * cs + idx];
+      for (int q = 0; q < NM; ++q) {
+        b23[q] = (R)e[q][E_B23]; ef[q] = (R)e[q][E_FULL]; qq[q] = (R)(dt * e[q][E_A41]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          n1[q][c] = ok[q] ? s.n1[c * cs + idx[q]] : czero<R>();
+          a[q][c] = ok[q] ? s.acc[c * cs + idx[q]] : czero<R>();
+        }
       }
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        s.acc[c * cs + idx] = cmk<R>(a[c].x + b23 * nl[c].x, a[c].y + b23 * nl[c].y);
-        const C2<R> dn = cmk<R>(R(2) * nl[c].x - n1[c].x, R(2) * nl[c].y - n1[c].y);
-        s.temp[c * cs + idx] = axpby<R>(ef, u[c], q, dn);
+      for (int q = 0; q < NM; ++q) {
+        if (!ok[q]) continue;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          s.acc[c * cs + idx[q]] = cmk<R>(a[q][c].x + b23[q] * nl[q][c].x, a[q][c].y + b23[q] * nl[q][c].y);
+          const C2<R> dn = cmk<R>(R(2) * nl[q][c].x - n1[q][c].x, R(2) * nl[q][c].y - n1[q][c].y);
+          s.temp[c * cs + idx[q]] = axpby<R>(ef[q], u[q][c], qq[q], dn);
+        }
       }
       break;
     }
     case ST_ETD_4: {  // solver.rs:354-378
-      const R b4 = (R)e[E_B4], ef = (R)e[E_FULL];
-      C2<R> a[3];
+      R b4[NM], ef[NM];
+      C2<R> a[NM][3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) a[c] = s.acc[c * cs + idx];
+      for (int q = 0; q < NM; ++q) {
+        b4[q] = (R)e[q][E_B4]; ef[q] = (R)e[q][E_FULL];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const C2<R> rhs = cmk<R>(a[c].x + b4 * nl[c].x, a[c].y + b4 * nl[c].y);
-        s.u_out[c * cs + idx] = axpby<R>(ef, u[c], (R)dt, rhs);
+        for (int c = 0; c < 3; ++c) a[q][c] = ok[q] ? s.acc[c * cs + idx[q]] : czero<R>();
       }
-      break;
-    }
-    case ST_ETD_CM_1: {  // textbook: a = E2 u + (h/2) phi1(z/2) N1
-      const R eh = (R)e[E_HALF], q = (R)(0.5 * dt * e[E_A21]);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        s.n1[c * cs + idx] = nl[c];
-        s.temp[c * cs + idx] = axpby<R>(eh, u[c], q, nl[c]);
-      }
-      break;
-    }
-    case ST_ETD_CM_2: {  // b = E2 u + (h/2) phi1(z/2) N2
-      const R b1 = (R)e[E_B1], b23 = (R)e[E_B23], eh = (R)e[E_HALF], q = (R)(0.5 * dt * e[E_A21]);
-      C2<R> n1[3];
+      for (int q = 0; q < NM; ++q) {
+        if (!ok[q]) continue;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) n1[c] = s.n1[c * cs + idx];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        s.acc[c * cs + idx] = axpby<R>(b1, n1[c], b23, nl[c]);
-        s.temp[c * cs + idx] = axpby<R>(eh, u[c], q, nl[c]);
+        for (int c = 0; c < 3; ++c) {
+          const C2<R> rhs = cmk<R>(a[q][c].x + b4[q] * nl[q][c].x, a[q][c].y + b4[q] * nl[q][c].y);
+          s.u_out[c * cs + idx[q]] = axpby<R>(ef[q], u[q][c], (R)dt, rhs);
+        }
       }
       break;
     }
     case ST_ETD_CM_3: {  // c = E2 a + (h/2) phi1(z/2) (2 N3 - N1), a rebuilt from u, N1
-      const R b23 = (R)e[E_B23], eh = (R)e[E_HALF], q = (R)(0.5 * dt * e[E_A21]);
-      C2<R> n1[3], ac[3];
+      R b23[NM], eh[NM], qq[NM];
+      C2<R> n1[NM][3], ac[NM][3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        n1[c] = s.n1[c * cs + idx];
-        ac[c] = s.acc[c * cs + idx];
+      for (int q = 0; q < NM; ++q) {
+        b23[q] = (R)e[q][E_B23]; eh[q] = (R)e[q][E_HALF]; qq[q] = (R)(0.5 * dt * e[q][E_A21]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          n1[q][c] = ok[q] ? s.n1[c * cs + idx[q]] : czero<R>();
+          ac[q][c] = ok[q] ? s.acc[c * cs + idx[q]] : czero<R>();
+        }
       }
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        s.acc[c * cs + idx] = cmk<R>(ac[c].x + b23 * nl[c].x, ac[c].y + b23 * nl[c].y);
-        const C2<R> a = axpby<R>(eh, u[c], q, n1[c]);
-        const C2<R> dn = cmk<R>(R(2) * nl[c].x - n1[c].x, R(2) * nl[c].y - n1[c].y);
-        s.temp[c * cs + idx] = axpby<R>(eh, a, q, dn);
+      for (int q = 0; q < NM; ++q) {
+        if (!ok[q]) continue;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          s.acc[c * cs + idx[q]] = cmk<R>(ac[q][c].x + b23[q] * nl[q][c].x, ac[q][c].y + b23[q] * nl[q][c].y);
+          const C2<R> av = axpby<R>(eh[q], u[q][c], qq[q], n1[q][c]);
+          const C2<R> dn = cmk<R>(R(2) * nl[q][c].x - n1[q][c].x, R(2) * nl[q][c].y - n1[q][c].y);
+          s.temp[c * cs + idx[q]] = axpby<R>(eh[q], av, qq[q], dn);
+        }
       }
       break;
     }
     default: break;
   }
+}
+
+template <typename R>
+__device__ __forceinline__ void stage_apply(const StageArgs<R>& s, size_t idx, int m, R k2, const C2<R>* nl) {
+  const C2<R> v[1][3] = {{nl[0], nl[1], nl[2]}};
+  const bool ok[1] = {true};
+  stage_apply_n<R, 1>(s, &idx, &m, &k2, v, ok);
 }
 
 

@@ -400,28 +400,44 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
     });
   }
   __syncthreads();
+  // FP32: two modes per iteration, so that the epilogue's loads of both are
+  // in flight together (FP64 keeps one: register budget, FP64-pipe bound)
+  constexpr int EM = sizeof(R) == 4 ? 2 : 1;
 #pragma unroll 1
-  for (int e = threadIdx.x; e < N * NLINES; e += NT) {
-    const int ix = e / NLINES, l = e % NLINES;
-    const int lam = blockIdx.x * NLINES + l;
-    if (lam >= a.nlines) continue;
-    const int iy = lam / H;
-    const int z = lam - iy * H;
-    const int kxi = signed_k(ix, N), kyi = signed_k(iy, N);
-    const R kx = a.ks * (R)kxi, ky = a.ks * (R)kyi, kz = a.ks * (R)z;
-    C2<R> nl[3] = {cscale<R>(keep[e], a.s_out), cscale<R>(keep[N * NLINES + e], a.s_out),
-                   cscale<R>(keep[2 * N * NLINES + e], a.s_out)};
-    const R k2 = (kx * kx + ky * ky) + kz * kz;
-    if (!(k2 < R(1e-30))) {
-      const R inv = R(1) / k2;
-      const C2<R> kd = cmk<R>((kx * nl[0].x + ky * nl[1].x) + kz * nl[2].x,
-                              (kx * nl[0].y + ky * nl[1].y) + kz * nl[2].y);
-      nl[0] = cmk<R>(nl[0].x - kx * kd.x * inv, nl[0].y - kx * kd.y * inv);
-      nl[1] = cmk<R>(nl[1].x - ky * kd.x * inv, nl[1].y - ky * kd.y * inv);
-      nl[2] = cmk<R>(nl[2].x - kz * kd.x * inv, nl[2].y - kz * kd.y * inv);
+  for (int e0 = threadIdx.x; e0 < N * NLINES; e0 += EM * NT) {
+    size_t idx[EM];
+    int mm[EM];
+    R kk[EM];
+    C2<R> nl[EM][3];
+    bool ok[EM];
+#pragma unroll
+    for (int q = 0; q < EM; ++q) {
+      const int e = e0 + q * NT;
+      const int ix = e / NLINES, l = e % NLINES;
+      const int lam = blockIdx.x * NLINES + l;
+      ok[q] = e < N * NLINES && lam < a.nlines;
+      const int iy = ok[q] ? lam / H : 0;
+      const int z = ok[q] ? lam - iy * H : 0;
+      const int kxi = signed_k(ok[q] ? ix : 0, N), kyi = signed_k(iy, N);
+      const R kx = a.ks * (R)kxi, ky = a.ks * (R)kyi, kz = a.ks * (R)z;
+      const int ee = ok[q] ? e : 0;
+      nl[q][0] = cscale<R>(keep[ee], a.s_out);
+      nl[q][1] = cscale<R>(keep[N * NLINES + ee], a.s_out);
+      nl[q][2] = cscale<R>(keep[2 * N * NLINES + ee], a.s_out);
+      const R k2 = (kx * kx + ky * ky) + kz * kz;
+      if (!(k2 < R(1e-30))) {
+        const R inv = R(1) / k2;
+        const C2<R> kd = cmk<R>((kx * nl[q][0].x + ky * nl[q][1].x) + kz * nl[q][2].x,
+                                (kx * nl[q][0].y + ky * nl[q][1].y) + kz * nl[q][2].y);
+        nl[q][0] = cmk<R>(nl[q][0].x - kx * kd.x * inv, nl[q][0].y - kx * kd.y * inv);
+        nl[q][1] = cmk<R>(nl[q][1].x - ky * kd.x * inv, nl[q][1].y - ky * kd.y * inv);
+        nl[q][2] = cmk<R>(nl[q][2].x - kz * kd.x * inv, nl[q][2].y - kz * kd.y * inv);
+      }
+      kk[q] = k2;
+      mm[q] = kxi * kxi + kyi * kyi + z * z;
+      idx[q] = ((size_t)(ok[q] ? ix : 0) * N + iy) * H + z;
     }
-    const int m = kxi * kxi + kyi * kyi + z * z;
-    stage_apply<R>(a.st, ((size_t)ix * N + iy) * H + z, m, k2, nl);
+    stage_apply_n<R, EM>(a.st, idx, mm, kk, nl, ok);
   }
 }
 

@@ -171,8 +171,10 @@ def pass_model(n: int) -> dict:
         "P2_y_inverse_pad_omega": (5 * mnh + 6 * mmh, 6 * m * h * lf),
         "P3_z_c2r_cross_r2c": (6 * mmh + 3 * mmh, 4.5 * m * m * lf + 9.0 * m * m * m),
         "P4_y_forward_trunc": (3 * mmh + 3 * mnh, 3 * m * h * lf),
-        # stage epilogue average over the four ETD stages: (6 + 9 + 12 + 6)/4 = 8.25 N^2H reads+writes
-        "P5_x_forward_trunc_leray_stage": (3 * mnh + 8.25 * nh, 3 * n * h * lf),
+        # stage epilogue average over the four ETD stages (u read in each):
+        # (R u W n1,temp) 9, (R u,n1 W acc,temp) 12, (R u,n1,acc W acc,temp) 15,
+        # (R u,acc W u) 9 -> 11.25 N^2H reads+writes
+        "P5_x_forward_trunc_leray_stage": (3 * mnh + 11.25 * nh, 3 * n * h * lf),
         "NX_ngrid_x_inverse": (6 * nh, 3 * n * h * nf),
         "NY_ngrid_y_inverse": (6 * nh, 3 * n * h * nf),
         "NZ_ngrid_z_c2r_max": (3 * nh, 1.5 * n * n * nf),

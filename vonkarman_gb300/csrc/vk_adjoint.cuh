@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(256) k_adj_cbar(CbarArgs<R> a) {
 
 // A1: fields 0..4 as P1 on x; fields 5..7 = x-inverse of Pad(c_bar source)
 // (k_adj_cbar).  Kinds: 0 = u_c, 1 = i kx u, 2 = c_bar.
-template <typename R> struct OpAdjXInv {
+template <typename R, int GN = 0, int GM = 0> struct OpAdjXInv {
   int nfields, hz;
   int N, M;
   R s_in, ks;
@@ -77,12 +77,13 @@ template <typename R> struct OpAdjXInv {
   static constexpr bool STAGED_ANY = false;
   template <int K> __host__ __device__ static constexpr bool staged() { return false; }
   static constexpr int NKIND = 3;
+  VK_GRID_DIMS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : f < 5 ? 1 : 2; }
   template <int K> __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
-    const int ix = unpad_pos(p, N, M);
+    const int ix = unpad_pos(p, n_(), m_());
     const C2<R>* src = K == 2 ? cb : in;
     const int c = K == 0 ? f : K == 1 ? f - 2 : f - 5;
-    return ix < 0 ? czero<R>() : src[(size_t)c * cs + ((size_t)ix * N + iy) * hz + z];
+    return ix < 0 ? czero<R>() : src[(size_t)c * cs + ((ix * n_() + iy) * h_() + z)];
   }
   template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int p, C2<R> v) const {
     if constexpr (K == 2) {
@@ -90,8 +91,8 @@ template <typename R> struct OpAdjXInv {
     } else {
       v = cscale<R>(v, s_in);
       if constexpr (K == 1) {
-        const int ix = unpad_pos(p, N, M);
-        const R kx = ks * (R)signed_k(ix < 0 ? 0 : ix, N);
+        const int ix = unpad_pos(p, n_(), m_());
+        const R kx = ks * (R)signed_k(ix < 0 ? 0 : ix, n_());
         v = cmk<R>(-kx * v.y, kx * v.x);
       }
       return v;
@@ -99,28 +100,31 @@ template <typename R> struct OpAdjXInv {
   }
   __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int iy, int z, int i, C2<R> v) const {
-    out[(size_t)f * fs + ((size_t)i * N + iy) * hz + z] = v;
+    out[(size_t)f * fs + ((i * n_() + iy) * h_() + z)] = v;
   }
 };
 
 // A2: fields 0..5 as P2 (u, omega), fields 6..8 = y-inverse of c_bar.
 // Kinds as P2, then one more for c_bar.
-template <typename R> struct OpAdjYInv {
-  OpYInv<R> base;   // reads input fields 0..4
+template <typename R, int GN = 0, int GM = 0> struct OpAdjYInv {
+  using Base = OpYInv<R, GN, GM>;
+  Base base;   // reads input fields 0..4
   int nfields, hz;
-  static constexpr bool STAGED_ANY = OpYInv<R>::STAGED_ANY;
-  static constexpr int KC = OpYInv<R>::NKIND;   // the c_bar kind
+  static constexpr bool STAGED_ANY = Base::STAGED_ANY;
+  static constexpr int MAX_L16 = 0;        // 8-line tiles (16 spill)
+  static constexpr int KC = Base::NKIND;   // the c_bar kind
   template <int K> __host__ __device__ static constexpr bool staged() {
-    return K < KC && OpYInv<R>::template staged<K>();
+    return K < KC && Base::template staged<K>();
   }
   static constexpr int NKIND = KC + 1;
+  __host__ __device__ __forceinline__ int h_() const { return base.h_(); }
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 6 ? base.kind(f) : KC; }
   template <int K> __device__ __forceinline__ auto load(int f, int x, int z, int p) const {
     if constexpr (K < KC) {
       return base.template load<K>(f, x, z, p);
     } else {
-      const int iy = unpad_pos(p, base.N, base.M);
-      return iy < 0 ? czero<R>() : base.in[(size_t)(f - 1) * base.fsin + ((size_t)x * base.N + iy) * hz + z];
+      const int iy = unpad_pos(p, base.n_(), base.m_());
+      return iy < 0 ? czero<R>() : base.in[(size_t)(f - 1) * base.fsin + ((x * base.n_() + iy) * base.h_() + z)];
     }
   }
   template <int K, class T> __device__ __forceinline__ C2<R> prep(int f, int x, int z, int p, const T& r) const {
@@ -132,7 +136,7 @@ template <typename R> struct OpAdjYInv {
   }
   __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
-    base.out[(size_t)f * base.fsout + ((size_t)x * base.M + i) * hz + z] = v;
+    base.out[(size_t)f * base.fsout + ((x * base.m_() + i) * base.h_() + z)] = v;
   }
 };
 
@@ -353,7 +357,7 @@ k_adj_p5(A5Args<R> a, const C2<R>* __restrict__ tw) {
   load_twtab<R, L, false, NT>(tw_s, tw);
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   C2<R>* acc = xb + rsmem_elems<R, L, NLINES>();   // 3 components x N x NLINES
-  const int H = a.H;
+  constexpr int H = N / 2 + 1;   // a.H of the launch
   {
     const int l = threadIdx.x % NLINES;
     const int lam = blockIdx.x * NLINES + l;
@@ -366,9 +370,9 @@ k_adj_p5(A5Args<R> a, const C2<R>* __restrict__ tw) {
     sfor<6>([&](auto cc) {
       constexpr int C = decltype(cc)::value;
       if (C > 0) __syncthreads();   // xb is reused
-      const C2<R>* src = a.in + (size_t)C * a.fsin + (size_t)iy * H + z;
+      const C2<R>* src = a.in + (size_t)C * a.fsin + (iy * H + z);
       fft_lines<R, L, false, NT, NLINES, MapInterleaved<R, L, NLINES>, false, true>(
-          xb, tw_s, [&](int, int p) { return src[(size_t)p * N * H]; }, PrepNone{},
+          xb, tw_s, [&](int, int p) { return src[p * (N * H)]; }, PrepNone{},
           [&](int, int p, C2<R> v) {
             const int ix = unpad_pos(p, N, L);
             if (ix < 0) return;

@@ -4,6 +4,7 @@
 #pragma once
 
 #include <algorithm>
+#include <type_traits>
 
 #include "vk_adjoint.cuh"
 #include "vk_lines.cuh"
@@ -33,15 +34,21 @@ inline cudaError_t prepare_kernel(size_t smem) {
 // Register-resident strided pass (k_lines): nouter * hz lines per field in
 // tiles of NLINES.
 // Lines per CTA: 8 (row segments of 64 bytes in FP32, 128 in FP64), and 16
-// for FP32 y passes without staged inputs (P4, NY: measured 6 % faster; the
-// staged P2 and the x passes measured slower with 16).
-template <typename R, int L, bool XAXIS, bool STAGED> struct NLof {
-  static constexpr int value = (!XAXIS && !STAGED && sizeof(R) == 4 && L <= 512) ? 16 : 8;
+// for FP32 passes without staged inputs up to Op::MAX_L16 points (default
+// 512; 384 for the x passes and for ops with paired raw loads, beyond which
+// the 16-line kernels spill).
+template <class Op, class = void> struct OpMaxL16 { static constexpr int value = 512; };
+template <class Op> struct OpMaxL16<Op, std::void_t<decltype(Op::MAX_L16)>> {
+  static constexpr int value = Op::MAX_L16;
+};
+template <typename R, int L, bool XAXIS, class Op> struct NLof {
+  static constexpr int LMAX = XAXIS ? cmin(384, OpMaxL16<Op>::value) : OpMaxL16<Op>::value;
+  static constexpr int value = (!Op::STAGED_ANY && sizeof(R) == 4 && L <= LMAX) ? 16 : 8;
 };
 
 template <typename R, int L, bool INV, bool XAXIS = false, class Op>
 inline cudaError_t launch_lines(const Op& op, int nouter, const C2<R>* tw, cudaStream_t s) {
-  constexpr int NLINES = NLof<R, L, XAXIS, Op::STAGED_ANY>::value;
+  constexpr int NLINES = NLof<R, L, XAXIS, Op>::value;
   constexpr int NT = cmin(rthreads<R, L, NLINES>(), 384);
   const size_t smem = lines_smem_bytes<R, L, NLINES>(op);
   constexpr auto kern = k_lines<R, L, INV, NLINES, NT, Op>;
@@ -70,14 +77,14 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   // P1
   {
     TimerScope ts(p.timer, PASS_P1, s);
-    OpXInv<R> o{5, H, N, M, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fsA1};
+    OpXInv<R, N, M> o{5, H, N, M, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fsA1};
     e = launch_lines<R, M, true, true>(o, N, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   // P2
   {
     TimerScope ts(p.timer, PASS_P2, s);
-    OpYInv<R> o{6, H, N, M, 0, ks, p.bufA, fsA1, p.bufB, fsB2};
+    OpYInv<R, N, M> o{6, H, N, M, 0, ks, p.bufA, fsA1, p.bufB, fsB2};
     e = launch_lines<R, M, true>(o, M, p.twM, s);
     if (e != cudaSuccess) return e;
   }
@@ -99,7 +106,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   // P4
   {
     TimerScope ts(p.timer, PASS_P4, s);
-    OpYFwdTrunc<R> o{3, H, N, M, p.bufA, fsA3, p.bufB, fsB4};
+    OpYFwdTrunc<R, N, M> o{3, H, N, M, p.bufA, fsA3, p.bufB, fsB4};
     e = launch_lines<R, M, false>(o, M, p.twM, s);
     if (e != cudaSuccess) return e;
   }
@@ -141,13 +148,13 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
     k_adj_cbar<R><<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(ca);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    OpAdjXInv<R> o{8, H, N, M, (R)(1.0 / ((double)N * N * N)), ks, p.x, p.cs, p.bufB, p.bufA, fsA1};
+    OpAdjXInv<R, N, M> o{8, H, N, M, (R)(1.0 / ((double)N * N * N)), ks, p.x, p.cs, p.bufB, p.bufA, fsA1};
     e = launch_lines<R, M, true, true>(o, N, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   {
     TimerScope ts(p.timer, PASS_A2, s);
-    OpAdjYInv<R> o{OpYInv<R>{6, H, N, M, 0, ks, p.bufA, fsA1, p.bufB, fsB2}, 9, H};
+    OpAdjYInv<R, N, M> o{OpYInv<R, N, M>{6, H, N, M, 0, ks, p.bufA, fsA1, p.bufB, fsB2}, 9, H};
     e = launch_lines<R, M, true>(o, M, p.twM, s);
     if (e != cudaSuccess) return e;
   }
@@ -167,7 +174,7 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
   }
   {
     TimerScope ts(p.timer, PASS_A4, s);
-    OpYFwdTrunc<R> o{6, H, N, M, p.bufA, fsA3, p.bufB, fsB4};
+    OpYFwdTrunc<R, N, M> o{6, H, N, M, p.bufA, fsA3, p.bufB, fsB4};
     e = launch_lines<R, M, false>(o, M, p.twM, s);
     if (e != cudaSuccess) return e;
   }
@@ -199,7 +206,7 @@ inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
   {
     TimerScope ts(p.timer, PASS_NX, s);
     const int nf = need_w ? 5 : 3;
-    OpXInv<R> o{nf, H, N, N, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fs};
+    OpXInv<R, N, N> o{nf, H, N, N, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fs};
     e = launch_lines<R, N, true, true>(o, N, p.twN, s);
     if (e != cudaSuccess) return e;
   }
@@ -207,7 +214,7 @@ inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
     TimerScope ts(p.timer, PASS_NY, s);
     const int nf = both ? 6 : 3;
     const int gbase = p.which == 2 ? 3 : 0;
-    OpYInv<R> o{nf, H, N, N, gbase, ks, p.bufA, fs, p.bufB, fs};
+    OpYInv<R, N, N> o{nf, H, N, N, gbase, ks, p.bufA, fs, p.bufB, fs};
     e = launch_lines<R, N, true>(o, N, p.twN, s);
     if (e != cudaSuccess) return e;
   }

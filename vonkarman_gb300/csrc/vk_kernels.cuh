@@ -51,11 +51,21 @@ __host__ __device__ constexpr int zthreads() { return cmax(64, cmin(1024, round3
 // warps per SM, which caps registers near 85 per thread.
 template <int NT> __host__ __device__ constexpr int min_blocks() { return cmax(1, 768 / NT); }
 
+// Grid sizes of a strided-pass op: compile-time when the op is instantiated
+// for one grid (GN > 0: N = GN, padded length M = GM, H = GN/2 + 1), so that
+// the zero-padding tests and index products fold per butterfly input; else
+// the runtime members N, M, hz.  Offsets inside one field fit in int (at most
+// (3N/2)^2 (N/2+1) < 2^31 elements for N <= 1024); the field base stays size_t.
+#define VK_GRID_DIMS(GN, GM)                                                            \
+  __host__ __device__ __forceinline__ int n_() const { return GN > 0 ? GN : N; }        \
+  __host__ __device__ __forceinline__ int m_() const { return GN > 0 ? GM : M; }        \
+  __host__ __device__ __forceinline__ int h_() const { return GN > 0 ? GN / 2 + 1 : hz; }
+
 // P1 / N-grid X: x-inverse of the spectral state, zero-pad N -> M (M == N on
 // the N grid).  Fields: 0..2 = u_c, 3 = i kx u_y, 4 = i kx u_z.  s_in folds the
 // 1/M^3 of the padded c2r and the (M/N)^3 pre-scale (dealiased.rs:43,:45-62)
 // into one factor 1/N^3.  Kinds: 0 = u_c, 1 = i kx u.
-template <typename R> struct OpXInv {
+template <typename R, int GN = 0, int GM = 0> struct OpXInv {
   int nfields, hz;
   int N, M;
   R s_in, ks;
@@ -64,24 +74,25 @@ template <typename R> struct OpXInv {
   static constexpr bool STAGED_ANY = false;
   template <int K> __host__ __device__ static constexpr bool staged() { return false; }
   static constexpr int NKIND = 2;
+  VK_GRID_DIMS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : 1; }
   template <int K> __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
-    const int ix = unpad_pos(p, N, M);
+    const int ix = unpad_pos(p, n_(), m_());
     const int c = K == 0 ? f : f - 2;
-    return ix < 0 ? czero<R>() : in[(size_t)c * cs + ((size_t)ix * N + iy) * hz + z];
+    return ix < 0 ? czero<R>() : in[(size_t)c * cs + ((ix * n_() + iy) * h_() + z)];
   }
   template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int p, C2<R> v) const {
     v = cscale<R>(v, s_in);
     if constexpr (K == 1) {
-      const int ix = unpad_pos(p, N, M);
-      const R kx = ks * (R)signed_k(ix < 0 ? 0 : ix, N);
+      const int ix = unpad_pos(p, n_(), m_());
+      const R kx = ks * (R)signed_k(ix < 0 ? 0 : ix, n_());
       v = cmk<R>(-kx * v.y, kx * v.x);
     }
     return v;
   }
   __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int iy, int z, int i, C2<R> v) const {
-    out[(size_t)f * fs + ((size_t)i * N + iy) * hz + z] = v;
+    out[(size_t)f * fs + ((i * n_() + iy) * h_() + z)] = v;
   }
 };
 
@@ -90,18 +101,20 @@ template <typename R> struct OpXInv {
 // (curl: vonkarman-core/src/spectral_ops.rs:81-108).  kx was applied in P1, ky
 // and kz are applied here (both are constant along an x line).  Kind 0 = u
 // (one load per position).  Omega needs two operand fields per position:
-// in FP32 one kind (1) stages them through shared memory; in FP64, whose
-// residency the staging tile would halve, kinds 1..3 (g = 3..5) combine them
-// at the load.
-template <typename R> struct OpYInv {
+// in FP32 one kind (1) loads both raw operands (issued before any arithmetic,
+// in chunks) and forms omega in prep; in FP64, whose registers the raw pairs
+// would overflow, kinds 1..3 (g = 3..5) combine them at the load.
+template <typename R, int GN = 0, int GM = 0> struct OpYInv {
   int nfields, hz;
   int N, M, gbase;
   R ks;
   const C2<R>* in; size_t fsin;   // (M, N, H): Ux, Uy, Uz, Vy, Vz
   C2<R>* out; size_t fsout;       // (M, M, H)
-  static constexpr bool STAGED_ANY = sizeof(R) == 4;
-  template <int K> __host__ __device__ static constexpr bool staged() { return K == 1 && sizeof(R) == 4; }
+  static constexpr bool STAGED_ANY = false;
+  static constexpr int MAX_L16 = 384;   // 16-line tiles up to this length (FP32; longer ones spill)
+  template <int K> __host__ __device__ static constexpr bool staged() { return false; }
   static constexpr int NKIND = sizeof(R) == 4 ? 2 : 4;
+  VK_GRID_DIMS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const {
     const int g = f + gbase;
     return g < 3 ? 0 : sizeof(R) == 4 ? 1 : g - 2;
@@ -110,15 +123,15 @@ template <typename R> struct OpYInv {
   __device__ __forceinline__ static int opa(int g) { return g == 3 ? 1 : 0; }
   __device__ __forceinline__ static int opb(int g) { return g == 3 ? 2 : g == 4 ? 4 : 3; }
   __device__ __forceinline__ C2<R> omega(int g, int z, int iy, const C2x2<R>& r) const {
-    const R ky = ks * (R)signed_k(iy, N);
+    const R ky = ks * (R)signed_k(iy, n_());
     const R kz = ks * (R)z;
     if (g == 3) return cmul_i<R>(cmk<R>(ky * r.b.x - kz * r.a.x, ky * r.b.y - kz * r.a.y));  // i (ky Uz - kz Uy)
     if (g == 4) return cmk<R>(-kz * r.a.y - r.b.x, kz * r.a.x - r.b.y);                     // i kz Ux - Vz
     return cmk<R>(r.b.x + ky * r.a.y, r.b.y - ky * r.a.x);                                  // Vy - i ky Ux
   }
   template <int K> __device__ __forceinline__ auto load(int f, int x, int z, int p) const {
-    const int iy = unpad_pos(p, N, M);
-    const C2<R>* s = in + ((size_t)x * N + (iy < 0 ? 0 : iy)) * hz + z;
+    const int iy = unpad_pos(p, n_(), m_());
+    const C2<R>* s = in + ((x * n_() + (iy < 0 ? 0 : iy)) * h_() + z);
     if constexpr (K == 0) {
       return iy < 0 ? czero<R>() : s[(size_t)(f + gbase) * fsin];
     } else if constexpr (sizeof(R) == 8) {
@@ -140,18 +153,18 @@ template <typename R> struct OpYInv {
   }
   template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int, C2<R> v) const { return v; }
   template <int K> __device__ __forceinline__ C2<R> prep(int f, int, int z, int p, const C2x2<R>& r) const {
-    const int iy = unpad_pos(p, N, M);
+    const int iy = unpad_pos(p, n_(), m_());
     return omega(f + gbase, z, iy < 0 ? 0 : iy, r);
   }
   __device__ __forceinline__ int out_index(int p) const { return p; }
   __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
-    out[(size_t)f * fsout + ((size_t)x * M + i) * hz + z] = v;
+    out[(size_t)f * fsout + ((x * m_() + i) * h_() + z)] = v;
   }
 };
 
 // P4: y-forward of the three cross-product fields, keep N of M modes
 // (truncate_spectral, dealiased.rs:141-163).
-template <typename R> struct OpYFwdTrunc {
+template <typename R, int GN = 0, int GM = 0> struct OpYFwdTrunc {
   int nfields, hz;
   int N, M;
   const C2<R>* in; size_t fsin;   // (M, M, H)
@@ -159,14 +172,15 @@ template <typename R> struct OpYFwdTrunc {
   static constexpr bool STAGED_ANY = false;
   template <int K> __host__ __device__ static constexpr bool staged() { return false; }
   static constexpr int NKIND = 1;
+  VK_GRID_DIMS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int) const { return 0; }
   template <int K> __device__ __forceinline__ C2<R> load(int f, int x, int z, int p) const {
-    return in[(size_t)f * fsin + ((size_t)x * M + p) * hz + z];
+    return in[(size_t)f * fsin + ((x * m_() + p) * h_() + z)];
   }
   template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int, C2<R> v) const { return v; }
-  __device__ __forceinline__ int out_index(int p) const { return unpad_pos(p, N, M); }
+  __device__ __forceinline__ int out_index(int p) const { return unpad_pos(p, n_(), m_()); }
   __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {
-    out[(size_t)f * fsout + ((size_t)x * N + i) * hz + z] = v;
+    out[(size_t)f * fsout + ((x * n_() + i) * h_() + z)] = v;
   }
 };
 
@@ -179,6 +193,8 @@ template <typename R, int AXIS> struct OpPlainC2C {
   static constexpr bool STAGED_ANY = false;
   template <int K> __host__ __device__ static constexpr bool staged() { return false; }
   static constexpr int NKIND = 1;
+  static constexpr int MAX_L16 = 384;   // 16-line tiles up to this length (FP32; longer ones spill)
+  __host__ __device__ __forceinline__ int h_() const { return hz; }
   __host__ __device__ __forceinline__ int kind(int) const { return 0; }
   __device__ __forceinline__ size_t at(int outer, int z, int p) const {
     return AXIS == 0 ? ((size_t)p * ny + outer) * hz + z : ((size_t)outer * ny + p) * hz + z;

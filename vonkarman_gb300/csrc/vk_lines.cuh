@@ -298,8 +298,8 @@ __global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op o
   const int tile = blockIdx.x / op.nfields;
   const int lam = tile * NLINES + (int)(threadIdx.x % NLINES);
   const bool ok = lam < nlines;
-  const int outer = ok ? lam / op.hz : 0;
-  const int z = ok ? lam - outer * op.hz : 0;
+  const int outer = ok ? lam / op.h_() : 0;
+  const int z = ok ? lam - outer * op.h_() : 0;
   const int kd = op.kind(f);
   auto st = [&](int, int p, C2<R> v) {
     const int i = op.out_index(p);
@@ -381,7 +381,7 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
   load_twtab<R, L, false, NT>(tw_s, tw);
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   C2<R>* keep = xb + rsmem_elems<R, L, NLINES>();   // 3 fields x N x NLINES
-  const int H = a.H;
+  constexpr int H = N / 2 + 1;   // a.H of the launch
   {
     const int lam = blockIdx.x * NLINES + (int)(threadIdx.x % NLINES);
     const bool ok = lam < a.nlines;
@@ -390,9 +390,9 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
     sfor<3>([&](auto cc) {
       constexpr int C = decltype(cc)::value;
       if (C > 0) __syncthreads();   // xb is reused
-      const C2<R>* src = a.in + (size_t)C * a.fsin + (size_t)iy * H + z;
+      const C2<R>* src = a.in + (size_t)C * a.fsin + (iy * H + z);
       fft_lines<R, L, false, NT, NLINES, MapInterleaved<R, L, NLINES>, false, true>(
-          xb, tw_s, [&](int, int p) { return src[(size_t)p * N * H]; }, PrepNone{},
+          xb, tw_s, [&](int, int p) { return src[p * (N * H)]; }, PrepNone{},
           [&](int, int p, C2<R> v) {
             const int ix = unpad_pos(p, N, L);
             if (ix >= 0) keep[(C * N + ix) * NLINES + (int)(threadIdx.x % NLINES)] = v;

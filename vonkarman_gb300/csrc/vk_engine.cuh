@@ -114,7 +114,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   {
     TimerScope ts(p.timer, PASS_P5, s);
     constexpr int NL = P5Lines<R>::value;
-    constexpr int NT = cmin(rthreads<R, M, NL>(), 384);
+    constexpr int NT = p5_threads<R, M, NL>();
     const int nlines = N * H;
     const size_t smem = (size_t)(rsmem_elems<R, M, NL>() + 3 * N * NL) * sizeof(C2<R>);
     constexpr auto kern = k_p5<R, M, NL, NT>;

@@ -370,9 +370,21 @@ template <typename R> struct P5Args {
 };
 
 template <typename R> struct P5Lines { static constexpr int value = sizeof(R) == 8 ? 4 : 8; };
+// Threads of k_p5: one butterfly per thread in the widest FFT stage; FP32 up
+// to 384 points doubles them (measured 4 % faster at 384: the epilogue keeps
+// the same modes in flight per CTA with one mode per thread, and twice the
+// warps hide its arithmetic), two CTAs per SM.
+template <typename R, int L, int NLINES>
+__host__ __device__ constexpr int p5_threads() {
+  return sizeof(R) == 4 && L <= 384 ? cmin(2 * rthreads<R, L, NLINES>(), 384) : cmin(rthreads<R, L, NLINES>(), 384);
+}
+template <typename R, int L, int NLINES, int NT>
+__host__ __device__ constexpr int p5_min_blocks() {
+  return NT >= 2 * rthreads<R, L, NLINES>() ? 2 : lines_min_blocks<R, L, NT, true>();
+}
 
 template <typename R, int L, int NLINES, int NT>
-__global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT, true>())
+__global__ void __launch_bounds__(NT, p5_min_blocks<R, L, NLINES, NT>())
 k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int N = 2 * L / 3;
   static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
@@ -400,9 +412,10 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
     });
   }
   __syncthreads();
-  // FP32: two modes per iteration, so that the epilogue's loads of both are
-  // in flight together (FP64 keeps one: register budget, FP64-pipe bound)
-  constexpr int EM = sizeof(R) == 4 ? 2 : 1;
+  // FP32 with the FFT's thread count: two modes per iteration, so that the
+  // epilogue's loads of both are in flight together (FP64 keeps one: register
+  // budget, FP64-pipe bound; doubled threads keep one)
+  constexpr int EM = sizeof(R) == 4 && NT < 2 * rthreads<R, L, NLINES>() ? 2 : 1;
 #pragma unroll 1
   for (int e0 = threadIdx.x; e0 < N * NLINES; e0 += EM * NT) {
     size_t idx[EM];

@@ -193,8 +193,8 @@ def step_bytes(n: int, elem: int) -> float:
 # ncu captures (dram__bytes_read.sum + dram__bytes_write.sum): FP64 at N=128,
 # FP32-bulk at N=256, scaled to grid n by the padded columns x modes (M^2 H).
 NCU_TRAFFIC = {
-    ("P3_z_c2r_cross_r2c", "fp64"): (128, 230115840 + 85875200),
-    ("P3_z_c2r_cross_r2c", "fp32bulk"): (256, 913084160 + 426719744),
+    ("P3_z_c2r_cross_r2c", "fp64"): (128, 230142720 + 85930752),
+    ("P3_z_c2r_cross_r2c", "fp32bulk"): (256, 913160192 + 426381056),
 }
 
 

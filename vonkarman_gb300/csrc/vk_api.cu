@@ -534,7 +534,7 @@ int vk_create(const vk_config* cfg, vk_ctx** out) {
   // spectrum shells: ceil(sqrt(3 (N/2)^2)) + 1 (spectrum.rs:22-26)
   const double kmx = (double)(n / 2);
   c->n_shells = (int)std::ceil(std::sqrt(kmx * kmx + kmx * kmx + kmx * kmx)) + 1;
-  c->red_blocks = 2 * c->dev_sms;
+  c->red_blocks = 8 * c->dev_sms;   // reduction CTAs: 8 per SM keep the state read in flight
   const size_t width = std::max(4, c->n_shells);
   if ((e = cudaMalloc(&c->part, (size_t)c->red_blocks * width * sizeof(double))) != cudaSuccess)
     return bail(e, "cudaMalloc(partials)");

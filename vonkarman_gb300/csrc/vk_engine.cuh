@@ -382,22 +382,42 @@ cudaError_t Engine<R>::fft_c2r(const FftParams<R>& p, cudaStream_t s) {
   return fz_dispatch<R>(p, true, scale, s);
 }
 
+#define VK_FOR_GRIDS(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512)
+
 template <typename R>
 cudaError_t Engine<R>::tier1_partial(const C2<R>* u, size_t cs, int N, double ks, double* part, int nblk,
                                      cudaStream_t s) {
-  k_tier1_partial<R><<<nblk, RED_THREADS, 0, s>>>(u, cs, N, N / 2 + 1, ks, part);
+  switch (N) {
+#define VK_CASE(G) \
+  case G: k_tier1_partial<R, G><<<nblk, RED_THREADS, 0, s>>>(u, cs, ks, part); break;
+    VK_FOR_GRIDS(VK_CASE)
+#undef VK_CASE
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+template <typename R, int G>
+inline cudaError_t spectrum_partial_n(const C2<R>* u, size_t cs, double ks, int nsh, double* part, int nblk,
+                                      cudaStream_t s) {
+  const size_t smem = (size_t)nsh * sizeof(double);
+  constexpr auto kern = k_spectrum_partial<R, G>;
+  cudaError_t e = prepare_kernel<kern>(smem);
+  if (e != cudaSuccess) return e;
+  kern<<<nblk, RED_THREADS, smem, s>>>(u, cs, ks, nsh, part);
   return cudaGetLastError();
 }
 
 template <typename R>
 cudaError_t Engine<R>::spectrum_partial(const C2<R>* u, size_t cs, int N, double ks, int nsh, double* part,
                                         int nblk, cudaStream_t s) {
-  const size_t smem = (size_t)nsh * sizeof(double);
-  constexpr auto kern = k_spectrum_partial<R>;
-  cudaError_t e = prepare_kernel<kern>(smem);
-  if (e != cudaSuccess) return e;
-  kern<<<nblk, RED_THREADS, smem, s>>>(u, cs, N, N / 2 + 1, ks, nsh, part);
-  return cudaGetLastError();
+  switch (N) {
+#define VK_CASE(G) \
+  case G: return spectrum_partial_n<R, G>(u, cs, ks, nsh, part, nblk, s);
+    VK_FOR_GRIDS(VK_CASE)
+#undef VK_CASE
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace vk

@@ -74,8 +74,6 @@ template <typename R, int GN = 0, int GM = 0> struct OpAdjXInv {
   const C2<R>* in; size_t cs;          // stage input x
   const C2<R>* cb;                     // c_bar source (3 components, stride cs)
   C2<R>* out; size_t fs;
-  static constexpr bool STAGED_ANY = false;
-  template <int K> __host__ __device__ static constexpr bool staged() { return false; }
   static constexpr int NKIND = 3;
   VK_GRID_DIMS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : f < 5 ? 1 : 2; }
@@ -110,12 +108,8 @@ template <typename R, int GN = 0, int GM = 0> struct OpAdjYInv {
   using Base = OpYInv<R, GN, GM>;
   Base base;   // reads input fields 0..4
   int nfields, hz;
-  static constexpr bool STAGED_ANY = Base::STAGED_ANY;
   static constexpr int MAX_L16 = 0;        // 8-line tiles (16 spill)
   static constexpr int KC = Base::NKIND;   // the c_bar kind
-  template <int K> __host__ __device__ static constexpr bool staged() {
-    return K < KC && Base::template staged<K>();
-  }
   static constexpr int NKIND = KC + 1;
   __host__ __device__ __forceinline__ int h_() const { return base.h_(); }
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 6 ? base.kind(f) : KC; }

@@ -34,28 +34,25 @@ inline cudaError_t prepare_kernel(size_t smem) {
 // Register-resident strided pass (k_lines): nouter * hz lines per field in
 // tiles of NLINES.
 // Lines per CTA: 8 (row segments of 64 bytes in FP32, 128 in FP64), and 16
-// for FP32 passes without staged inputs up to Op::MAX_L16 points (default
-// 512; 384 for the x passes and for ops with paired raw loads, beyond which
-// the 16-line kernels spill).
+// for FP32 passes up to Op::MAX_L16 points (default 512; 384 for the x
+// passes and for ops with paired raw loads, beyond which the 16-line kernels
+// spill; 0 for ops that always take 8).
 template <class Op, class = void> struct OpMaxL16 { static constexpr int value = 512; };
 template <class Op> struct OpMaxL16<Op, std::void_t<decltype(Op::MAX_L16)>> {
   static constexpr int value = Op::MAX_L16;
 };
 template <typename R, int L, bool XAXIS, class Op> struct NLof {
   static constexpr int LMAX = XAXIS ? cmin(384, OpMaxL16<Op>::value) : OpMaxL16<Op>::value;
-  static constexpr int value = (!Op::STAGED_ANY && sizeof(R) == 4 && L <= LMAX) ? 16 : 8;
+  static constexpr int value = (sizeof(R) == 4 && L <= LMAX) ? 16 : 8;
 };
 
 template <typename R, int L, bool INV, bool XAXIS = false, class Op>
 inline cudaError_t launch_lines(const Op& op, int nouter, const C2<R>* tw, cudaStream_t s) {
   constexpr int NLINES = NLof<R, L, XAXIS, Op>::value;
   constexpr int NT = cmin(rthreads<R, L, NLINES>(), 384);
-  const size_t smem = lines_smem_bytes<R, L, NLINES>(op);
+  const size_t smem = (size_t)rsmem_elems<R, L, NLINES>() * sizeof(C2<R>);
   constexpr auto kern = k_lines<R, L, INV, NLINES, NT, Op>;
-  // the attribute is sized for the staging tile, so that launches of the
-  // same kernel without it do not need a second setting
-  cudaError_t e = prepare_kernel<kern>((size_t)(rsmem_elems<R, L, NLINES>() + (Op::STAGED_ANY ? L * NLINES : 0)) *
-                                       sizeof(C2<R>));
+  cudaError_t e = prepare_kernel<kern>(smem);
   if (e != cudaSuccess) return e;
   const int nlines = nouter * op.hz;
   const int ntiles = (nlines + NLINES - 1) / NLINES;

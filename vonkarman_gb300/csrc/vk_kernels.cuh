@@ -71,8 +71,6 @@ template <typename R, int GN = 0, int GM = 0> struct OpXInv {
   R s_in, ks;
   const C2<R>* in; size_t cs;
   C2<R>* out; size_t fs;
-  static constexpr bool STAGED_ANY = false;
-  template <int K> __host__ __device__ static constexpr bool staged() { return false; }
   static constexpr int NKIND = 2;
   VK_GRID_DIMS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : 1; }
@@ -110,9 +108,7 @@ template <typename R, int GN = 0, int GM = 0> struct OpYInv {
   R ks;
   const C2<R>* in; size_t fsin;   // (M, N, H): Ux, Uy, Uz, Vy, Vz
   C2<R>* out; size_t fsout;       // (M, M, H)
-  static constexpr bool STAGED_ANY = false;
   static constexpr int MAX_L16 = 384;   // 16-line tiles up to this length (FP32; longer ones spill)
-  template <int K> __host__ __device__ static constexpr bool staged() { return false; }
   static constexpr int NKIND = sizeof(R) == 4 ? 2 : 4;
   VK_GRID_DIMS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const {
@@ -169,8 +165,6 @@ template <typename R, int GN = 0, int GM = 0> struct OpYFwdTrunc {
   int N, M;
   const C2<R>* in; size_t fsin;   // (M, M, H)
   C2<R>* out; size_t fsout;       // (M, N, H)
-  static constexpr bool STAGED_ANY = false;
-  template <int K> __host__ __device__ static constexpr bool staged() { return false; }
   static constexpr int NKIND = 1;
   VK_GRID_DIMS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int) const { return 0; }
@@ -190,8 +184,6 @@ template <typename R, int AXIS> struct OpPlainC2C {
   int nfields, hz;
   int nx, ny;
   C2<R>* data;
-  static constexpr bool STAGED_ANY = false;
-  template <int K> __host__ __device__ static constexpr bool staged() { return false; }
   static constexpr int NKIND = 1;
   static constexpr int MAX_L16 = 384;   // 16-line tiles up to this length (FP32; longer ones spill)
   __host__ __device__ __forceinline__ int h_() const { return hz; }

@@ -280,19 +280,14 @@ __device__ __forceinline__ void load_twtab(C2<R>* tab, const C2<R>* __restrict__
 // empty.  Op supplies kind(f) in [0, NKIND) (fields of one kind share their
 // load/prep code, which is specialised per kind), load<K>(f, outer, z, p)
 // (memory loads only, zero for padded positions), prep<K>(f, outer, z, p,
-// raw), staged<K>() (stage the combined inputs in shared memory first),
-// out_index(p) (-1: dropped) and store(f, outer, z, i, v).  Lines past the
-// end (lam >= nlines) load line 0 and store nothing.
+// raw), out_index(p) (-1: dropped) and store(f, outer, z, i, v).  Lines past
+// the end (lam >= nlines) load line 0 and store nothing.
 template <typename R, int L, bool INV, int NLINES, int NT, class Op>
 __global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op op, const C2<R>* __restrict__ tw, int nlines) {
   static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
   extern __shared__ __align__(16) unsigned char vk_smem[];
-  // ops that stage inputs through shared memory keep their twiddles in the
-  // global table (measured faster: their shared-memory pipe is the busier one)
-  constexpr bool TWS = !Op::STAGED_ANY;
-  __shared__ C2<R> tw_sm[TWS ? twtab_elems<R, false>(L) : 1];
-  if constexpr (TWS) load_twtab<R, L, false, NT>(tw_sm, tw);
-  const C2<R>* tw_s = TWS ? tw_sm : tw;
+  __shared__ C2<R> tw_s[twtab_elems<R, false>(L)];
+  load_twtab<R, L, false, NT>(tw_s, tw);
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   const int f = blockIdx.x % op.nfields;
   const int tile = blockIdx.x / op.nfields;
@@ -308,50 +303,10 @@ __global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op o
   sfor<Op::NKIND>([&](auto kc) {
     constexpr int K = decltype(kc)::value;
     if (kd != K) return;   // uniform over the CTA
-    if constexpr (Op::template staged<K>()) {
-      // Inputs that combine several loads per position: every thread loads
-      // its share of the tile (positions tid / NLINES + i NT / NLINES of its
-      // own line), combines, and stages the result in shared memory; the
-      // first stage then reads shared memory.
-      C2<R>* sin = xb + rsmem_elems<R, L, NLINES>();
-      constexpr int PER = (L * NLINES + NT - 1) / NT;
-      const int l = threadIdx.x % NLINES;
-      using Raw = decltype(op.template load<K>(f, outer, z, 0));
-      Raw raw[PER];
-#pragma unroll
-      for (int i = 0; i < PER; ++i) {
-        const int p = (int)threadIdx.x / NLINES + i * (NT / NLINES);
-        if (p < L) raw[i] = op.template load<K>(f, outer, z, p);
-      }
-#pragma unroll
-      for (int i = 0; i < PER; ++i) {
-        const int p = (int)threadIdx.x / NLINES + i * (NT / NLINES);
-        if (p < L) sin[p * NLINES + l] = op.template prep<K>(f, outer, z, p, raw[i]);
-      }
-      __syncthreads();
-      fft_lines<R, L, INV, NT, NLINES, MapInterleaved<R, L, NLINES>, false, TWS>(
-          xb, tw_s, [&](int ll, int p) { return sin[p * NLINES + ll]; }, PrepNone{}, st);
-    } else {
-      fft_lines<R, L, INV, NT, NLINES, MapInterleaved<R, L, NLINES>, false, TWS>(
-          xb, tw_s, [&](int, int p) { return op.template load<K>(f, outer, z, p); },
-          [&](int, int p, const auto& raw) { return op.template prep<K>(f, outer, z, p, raw); }, st);
-    }
+    fft_lines<R, L, INV, NT, NLINES, MapInterleaved<R, L, NLINES>, false, true>(
+        xb, tw_s, [&](int, int p) { return op.template load<K>(f, outer, z, p); },
+        [&](int, int p, const auto& raw) { return op.template prep<K>(f, outer, z, p, raw); }, st);
   });
-}
-// shared memory of k_lines: the exchange buffer, plus a staging tile when a
-// field of this launch has a staged kind
-template <int K, class Op> inline bool kind_staged(int k) {
-  if constexpr (K >= Op::NKIND) {
-    return false;
-  } else {
-    return k == K ? Op::template staged<K>() : kind_staged<K + 1, Op>(k);
-  }
-}
-template <typename R, int L, int NLINES, class Op>
-inline size_t lines_smem_bytes(const Op& op) {
-  bool staged = false;
-  for (int f = 0; f < op.nfields; ++f) staged = staged || kind_staged<0, Op>(op.kind(f));
-  return (size_t)(rsmem_elems<R, L, NLINES>() + (staged ? L * NLINES : 0)) * sizeof(C2<R>);
 }
 
 // ---------------------------------------------------------------------------

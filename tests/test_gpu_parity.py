@@ -301,6 +301,34 @@ def test_tier1_and_spectrum_vs_oracle(vk):
     assert s.cfl_dt() == pytest.approx(ref.compute_cfl_dt(), rel=1e-13)
 
 
+@pytest.mark.parametrize("n,l,prec", [(32, 3.0, "fp64"), (64, 2.0 * math.pi, "fp32bulk"), (64, 5.0, "fp32bulk")])
+def test_tier1_and_spectrum_box_lengths_and_precisions(vk, n, l, prec):
+    """Diagnostics of the initial state against the oracle, on boxes whose
+    wavenumber scale is not 1 (shells from the FP64 |k| path) and in the
+    FP32-bulk form (per-mode products in FP32, FP64 sums).  Helicity and
+    superhelicity can cancel far below their bounds, so their error is
+    measured against sqrt(E Omega) and kmax Omega."""
+    g = vo.Grid(n, l)
+    u0 = vo.hermitian_clean(g, vo.random_field(g, 11, amp=200.0))
+    ref = vo.Periodic3D(g, 0.01, u0)
+    s = vk.Periodic3D(vk.GridSpec(n, l), 0.01, u0, vk.SolverOptions(precision=prec))
+    want = ref.tier1()
+    got = s.tier1()
+    tol = TOL_DIAG if prec == "fp64" else 1e-6
+    kmax = (2.0 * math.pi / l) * (n // 2)
+    scale = {"helicity": math.sqrt(want["energy"] * want["enstrophy"]),
+             "superhelicity": kmax * want["enstrophy"],
+             "helicity_dissipation_rate": 2.0 * 0.01 * kmax * want["enstrophy"]}
+    for k in ("energy", "enstrophy", "helicity", "superhelicity", "max_vorticity", "energy_dissipation_rate",
+              "helicity_dissipation_rate", "cfl_number"):
+        v = want[k]
+        assert abs(getattr(got, k) - v) <= tol * max(abs(v), scale.get(k, 0.0)), (k, getattr(got, k), v)
+    shells, spec = vk.energy_spectrum(s)
+    sh_ref, spec_ref = vo.energy_spectrum(ref.u_hat, ref.ops)
+    assert np.array_equal(shells, sh_ref)
+    assert np.abs(spec - spec_ref).max() <= tol * np.abs(spec_ref).max()
+
+
 def test_restart_bitwise(vk):
     # solver.rs:673-706 / tests/checkpoint_restart.rs:10-63
     n = 16

@@ -249,7 +249,7 @@ k_adj_z(A3Args<R> a, const C2<R>* __restrict__ tw) {
 //   ADJ_U  (x = u): ub = acc + y
 // (ub = cotangent of the step's output, E = exp(z), E2 = exp(z/2)).
 // Inputs of all three components are loaded before any store (see
-// stage_apply).
+// stage_apply_n).
 template <typename R>
 __device__ __forceinline__ void adj_stage_apply(const AdjStageArgs<R>& s, size_t idx, int m, const C2<R>* y) {
   const size_t cs = s.cs;

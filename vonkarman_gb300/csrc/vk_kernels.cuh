@@ -388,12 +388,7 @@ __device__ __forceinline__ void stage_apply_n(const StageArgs<R>& s, const size_
   }
 }
 
-template <typename R>
-__device__ __forceinline__ void stage_apply(const StageArgs<R>& s, size_t idx, int m, R k2, const C2<R>* nl) {
-  const C2<R> v[1][3] = {{nl[0], nl[1], nl[2]}};
-  const bool ok[1] = {true};
-  stage_apply_n<R, 1>(s, &idx, &m, &k2, v, ok);
-}
+
 
 
 // ---------------------------------------------------------------------------

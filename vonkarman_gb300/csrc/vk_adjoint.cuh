@@ -76,6 +76,7 @@ template <typename R, int GN = 0, int GM = 0> struct OpAdjXInv {
   C2<R>* out; size_t fs;
   static constexpr int NKIND = 3;
   VK_GRID_DIMS(GN, GM)
+  VK_PAD_ZEROS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : f < 5 ? 1 : 2; }
   template <int K> __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
     const int ix = unpad_pos(p, n_(), m_());
@@ -109,6 +110,7 @@ template <typename R, int GN = 0, int GM = 0> struct OpAdjYInv {
   Base base;   // reads input fields 0..4
   int nfields, hz;
   static constexpr int MAX_L16 = 0;        // 8-line tiles (16 spill)
+  static constexpr int ZERO_LO = Base::ZERO_LO, ZERO_HI = Base::ZERO_HI;   // c_bar is padded too
   static constexpr int KC = Base::NKIND;   // the c_bar kind
   static constexpr int NKIND = KC + 1;
   __host__ __device__ __forceinline__ int h_() const { return base.h_(); }

@@ -169,11 +169,24 @@ __device__ __forceinline__ void rad2(C2<R>* v, const C2<R>* w) {
 
 // 4-point DFT of (a0, w_a a1, w_b a2, w_c a3) where the pairs (a0, a2) and
 // (a1, a3) form the first butterfly layer.  Outputs in natural order.
-template <typename R, bool INV, bool TW>
+// Z (untwiddled only): bit i set = input a_i is known to be zero (a
+// zero-padded position), so its first-layer additions are skipped.
+template <typename R, bool INV, bool TW, unsigned Z = 0u>
 __device__ __forceinline__ void rad4_core(C2<R> a0, C2<R> a1, C2<R> a2, C2<R> a3, C2<R> w1, C2<R> w2, C2<R> w3,
                                           C2<R>& y0, C2<R>& y1, C2<R>& y2, C2<R>& y3) {
+  static_assert(!TW || Z == 0u, "known-zero inputs only in untwiddled stages");
   C2<R> t0, t1, t2, t3;
-  if (TW) {
+  if constexpr (!TW && (Z & 5u) != 0u) {
+    if constexpr (Z & 4u) { t0 = a0; t1 = a0; } else { t0 = a2; t1 = cmk<R>(-a2.x, -a2.y); }
+    if constexpr (Z & 10u) {
+      if constexpr (Z & 8u) { t2 = a1; t3 = a1; } else { t2 = a3; t3 = cmk<R>(-a3.x, -a3.y); }
+    } else {
+      bfly<R>(a1, a3, t2, t3);
+    }
+  } else if constexpr (!TW && (Z & 10u) != 0u) {
+    bfly<R>(a0, a2, t0, t1);
+    if constexpr (Z & 8u) { t2 = a1; t3 = a1; } else { t2 = a3; t3 = cmk<R>(-a3.x, -a3.y); }
+  } else if (TW) {
     t0 = tw_fma<R, INV>(a0, w2, a2);
     t1 = twice_minus<R>(a0, t0);
     const C2<R> b1 = tw_mul<R, INV>(w1, a1);
@@ -188,9 +201,9 @@ __device__ __forceinline__ void rad4_core(C2<R> a0, C2<R> a1, C2<R> a2, C2<R> a3
   bfly<R>(t1, t3, y1, y3);
 }
 
-template <typename R, bool INV, bool TW>
+template <typename R, bool INV, bool TW, unsigned Z = 0u>
 __device__ __forceinline__ void rad4(C2<R>* v, const C2<R>* w) {
-  rad4_core<R, INV, TW>(v[0], v[1], v[2], v[3], w[1], w[2], w[3], v[0], v[1], v[2], v[3]);
+  rad4_core<R, INV, TW, Z>(v[0], v[1], v[2], v[3], w[1], w[2], w[3], v[0], v[1], v[2], v[3]);
 }
 
 template <typename R, bool INV, bool TW>
@@ -216,15 +229,20 @@ __device__ __forceinline__ void rad3(C2<R>* v, const C2<R>* w) {
   }
 }
 
-// radix-8 = two 4-point DFTs (even / odd inputs) and a W8 layer.
-template <typename R, bool INV, bool TW>
+// radix-8 = two 4-point DFTs (even / odd inputs) and a W8 layer.  Z: known-zero
+// inputs (bit r for v[r]) of an untwiddled stage.
+template <int B0, int B1, int B2, int B3>
+__host__ __device__ constexpr unsigned zbits4(unsigned z) {
+  return ((z >> B0) & 1u) | (((z >> B1) & 1u) << 1) | (((z >> B2) & 1u) << 2) | (((z >> B3) & 1u) << 3);
+}
+template <typename R, bool INV, bool TW, unsigned Z = 0u>
 __device__ __forceinline__ void rad8(C2<R>* v, const C2<R>* w) {
   const R h = R(0.70710678118654752440084436210484904);  // sqrt(2)/2
   const C2<R> one = cmk<R>(R(1), R(0));
   C2<R> e0, e1, e2, e3, o0, o1, o2, o3;
   // even inputs v0, v2, v4, v6 (twiddles w0 = 1, w2, w4, w6)
-  rad4_core<R, INV, TW>(v[0], v[2], v[4], v[6], TW ? w[2] : one, TW ? w[4] : one, TW ? w[6] : one,
-                        e0, e1, e2, e3);
+  rad4_core<R, INV, TW, zbits4<0, 2, 4, 6>(Z)>(v[0], v[2], v[4], v[6], TW ? w[2] : one, TW ? w[4] : one,
+                                              TW ? w[6] : one, e0, e1, e2, e3);
   // odd inputs v1, v3, v5, v7: fold w1 into the first pair's base
   if (TW) {
     const C2<R> b1 = tw_mul<R, INV>(w[1], v[1]);
@@ -237,7 +255,7 @@ __device__ __forceinline__ void rad8(C2<R>* v, const C2<R>* w) {
     bfly<R>(t0, t2, o0, o2);
     bfly<R>(t1, t3, o1, o3);
   } else {
-    rad4_core<R, INV, false>(v[1], v[3], v[5], v[7], one, one, one, o0, o1, o2, o3);
+    rad4_core<R, INV, false, zbits4<1, 3, 5, 7>(Z)>(v[1], v[3], v[5], v[7], one, one, one, o0, o1, o2, o3);
   }
   // W8 layer
   bfly<R>(e0, o0, v[0], v[4]);
@@ -352,7 +370,9 @@ __device__ __forceinline__ void sfor(F&& f) {
   sfor_impl(f, std::make_integer_sequence<int, N>{});
 }
 
-template <typename R, bool INV, int RAD, bool TW>
+// Z: bit r set = input v[r] is known to be zero (untwiddled radix-8/4 stages
+// skip its first-layer additions; other radices ignore it).
+template <typename R, bool INV, int RAD, bool TW, unsigned Z = 0u>
 __device__ __forceinline__ void dft(C2<R>* v, const C2<R>* w);
 
 // Composite radix RAD = A * B in registers (Cooley-Tukey): n = b + B a,
@@ -401,16 +421,16 @@ __device__ __forceinline__ void dft_comp(C2<R>* v, const C2<R>* w) {
   });
 }
 
-template <typename R, bool INV, int RAD, bool TW>
+template <typename R, bool INV, int RAD, bool TW, unsigned Z>
 __device__ __forceinline__ void dft(C2<R>* v, const C2<R>* w) {
   if constexpr (comp_a<RAD>() > 0) {
     dft_comp<R, INV, RAD, TW>(v, w);
   } else if constexpr (RAD == 16) {
     rad16<R, INV, TW>(v, w);
   } else if constexpr (RAD == 8) {
-    rad8<R, INV, TW>(v, w);
+    rad8<R, INV, TW, TW ? 0u : Z>(v, w);
   } else if constexpr (RAD == 4) {
-    rad4<R, INV, TW>(v, w);
+    rad4<R, INV, TW, TW ? 0u : Z>(v, w);
   } else if constexpr (RAD == 3) {
     rad3<R, INV, TW>(v, w);
   } else {

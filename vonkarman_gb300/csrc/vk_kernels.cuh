@@ -60,6 +60,11 @@ template <int NT> __host__ __device__ constexpr int min_blocks() { return cmax(1
   __host__ __device__ __forceinline__ int n_() const { return GN > 0 ? GN : N; }        \
   __host__ __device__ __forceinline__ int m_() const { return GN > 0 ? GM : M; }        \
   __host__ __device__ __forceinline__ int h_() const { return GN > 0 ? GN / 2 + 1 : hz; }
+// Zero-padded input positions [ZERO_LO, ZERO_HI) of the inverse passes with
+// the 3/2 pad (compile-time grids only).
+#define VK_PAD_ZEROS(GN, GM)                                                            \
+  static constexpr int ZERO_LO = GN > 0 && GN != GM ? GN / 2 : 0;                       \
+  static constexpr int ZERO_HI = GN > 0 && GN != GM ? GM - GN / 2 : 0;
 
 // P1 / N-grid X: x-inverse of the spectral state, zero-pad N -> M (M == N on
 // the N grid).  Fields: 0..2 = u_c, 3 = i kx u_y, 4 = i kx u_z.  s_in folds the
@@ -73,6 +78,7 @@ template <typename R, int GN = 0, int GM = 0> struct OpXInv {
   C2<R>* out; size_t fs;
   static constexpr int NKIND = 2;
   VK_GRID_DIMS(GN, GM)
+  VK_PAD_ZEROS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : 1; }
   template <int K> __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
     const int ix = unpad_pos(p, n_(), m_());
@@ -111,6 +117,7 @@ template <typename R, int GN = 0, int GM = 0> struct OpYInv {
   static constexpr int MAX_L16 = 384;   // 16-line tiles up to this length (FP32; longer ones spill)
   static constexpr int NKIND = sizeof(R) == 4 ? 2 : 4;
   VK_GRID_DIMS(GN, GM)
+  VK_PAD_ZEROS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const {
     const int g = f + gbase;
     return g < 3 ? 0 : sizeof(R) == 4 ? 1 : g - 2;

@@ -15,6 +15,8 @@
 // NLINES elements.
 #pragma once
 
+#include <type_traits>
+
 #include "vk_kernels.cuh"
 
 namespace vk {
@@ -138,7 +140,18 @@ struct MapContig {
   static constexpr int elems() { return NLINES * zpad_len<R>(L); }
 };
 
-template <typename R, int L, bool INV, int NT, int NLINES, class MAP, int S, int NS, bool SL = false, bool TT = false>
+// Inputs of the first stage at positions p in [Z0, Z1) are known to be zero
+// (zero-padded modes): butterflies whose input r lies there for every j (all
+// of [r NB, r NB + NB) inside the range) skip its first-layer additions.
+__host__ __device__ constexpr unsigned zero_mask(int nb, int rad, int z0, int z1) {
+  unsigned m = 0u;
+  for (int r = 0; r < rad && r < 32; ++r)
+    if (z0 < z1 && r * nb >= z0 && r * nb + nb <= z1) m |= 1u << r;
+  return m;
+}
+
+template <typename R, int L, bool INV, int NT, int NLINES, class MAP, int S, int NS, bool SL = false, bool TT = false,
+          int Z0 = 0, int Z1 = 0>
 struct RegStage {
   static constexpr int RAD = rradix<R, MAP::CONTIG>(L, S);
   static constexpr int NB = L / RAD;            // butterflies per line
@@ -221,7 +234,7 @@ struct RegStage {
             }
           }
         }
-        dft<R, INV, RAD, (S > 0)>(v[q], w);
+        dft<R, INV, RAD, (S > 0), S == 0 ? zero_mask(NB, RAD, Z0, Z1) : 0u>(v[q], w);
         const int base = (j - k) * RAD + k;
         if constexpr (LAST) {
 #pragma unroll
@@ -234,7 +247,7 @@ struct RegStage {
     }
     if constexpr (!LAST) {
       __syncthreads();
-      RegStage<R, L, INV, NT, NLINES, MAP, S + 1, NS * RAD, SL, TT>::run(xb, tw, ld, pp, st);
+      RegStage<R, L, INV, NT, NLINES, MAP, S + 1, NS * RAD, SL, TT, Z0, Z1>::run(xb, tw, ld, pp, st);
     }
   }
 };
@@ -246,11 +259,11 @@ struct RegStage {
 // also waits for all readers before storing.  TT: tw is the per-stage table
 // of load_twtab (shared memory), else the plain W_L^m table.
 template <typename R, int L, bool INV, int NT, int NLINES, class MAP = MapInterleaved<R, L, NLINES>, bool SL = false,
-          bool TT = false, class LD, class PP, class ST>
+          bool TT = false, int Z0 = 0, int Z1 = 0, class LD, class PP, class ST>
 __device__ __forceinline__ void fft_lines(C2<R>* xb, const C2<R>* __restrict__ tw, const LD& ld, const PP& pp,
                                           const ST& st) {
   static_assert(rstages<R>(L) > 0, "unsupported FFT length");
-  RegStage<R, L, INV, NT, NLINES, MAP, 0, 1, SL, TT>::run(xb, tw, ld, pp, st);
+  RegStage<R, L, INV, NT, NLINES, MAP, 0, 1, SL, TT, Z0, Z1>::run(xb, tw, ld, pp, st);
 }
 // pp for inputs that need no arithmetic after the load
 struct PrepNone {
@@ -274,6 +287,13 @@ __device__ __forceinline__ void load_twtab(C2<R>* tab, const C2<R>* __restrict__
     }
   }
 }
+
+// Positions [lo, hi) of a pass's input lines that are zero-padding for every
+// line (Op::ZERO_LO / ZERO_HI; none by default).
+template <class Op, class = void> struct OpZeroRange { static constexpr int lo = 0, hi = 0; };
+template <class Op> struct OpZeroRange<Op, std::void_t<decltype(Op::ZERO_LO)>> {
+  static constexpr int lo = Op::ZERO_LO, hi = Op::ZERO_HI;
+};
 
 // Generic strided pass: NLINES consecutive lines lam = outer * hz + z of one
 // field per CTA (blockIdx.x = f + nfields * tile), so no z tile is partly
@@ -303,7 +323,8 @@ __global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op o
   sfor<Op::NKIND>([&](auto kc) {
     constexpr int K = decltype(kc)::value;
     if (kd != K) return;   // uniform over the CTA
-    fft_lines<R, L, INV, NT, NLINES, MapInterleaved<R, L, NLINES>, false, true>(
+    fft_lines<R, L, INV, NT, NLINES, MapInterleaved<R, L, NLINES>, false, true, OpZeroRange<Op>::lo,
+              OpZeroRange<Op>::hi>(
         xb, tw_s, [&](int, int p) { return op.template load<K>(f, outer, z, p); },
         [&](int, int p, const auto& raw) { return op.template prep<K>(f, outer, z, p, raw); }, st);
   });
@@ -438,7 +459,8 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
   C2<R>* A = reinterpret_cast<C2<R>*>(vk_smem);
   C2<R>* B = A + NI * LP;
   const int col0 = blockIdx.x * 2 * CP;
-  fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>, false, true>(
+  // positions H .. M - H of the packed lines are the z zero-padding
+  fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>, false, true, H, M - H + 1>(
       A, tw_s,
       [&](int l, int p) -> C2x2<R> {
         const int t = l / (2 * CP);

@@ -173,11 +173,23 @@ int vk_nonlinear_host(vk_ctx* ctx, const double* ux, const double* uy, const dou
  * ceil(nsteps/nsnap) steps), and returns J = enstrophy of the final state
  * (the reference convention, solver.rs:436-465).  The state advances. */
 int vk_adjoint_forward(vk_ctx* ctx, int64_t nsteps, int32_t nsnap, double* J);
+/* Checkpoint schedule of the following vk_adjoint_forward / backward pairs.
+ * VK_ADJ_TWO_LEVEL (default): the level-1 checkpoints above, each segment
+ * recomputed once storing its stage inputs (nsnap + 4 ceil(nsteps/nsnap) + 1
+ * states; one recompute pass).  VK_ADJ_BINOMIAL: nsnap state slots (the
+ * initial state in one of them) reversed with the binomial treeverse schedule
+ * (nsnap + 4 states; each step recomputed at most r times, r the least with
+ * C(nsnap - 1 + r, r) >= nsteps), for adjoints the two-level schedule cannot
+ * hold in memory.  Both give the same gradient. */
+#define VK_ADJ_TWO_LEVEL 0
+#define VK_ADJ_BINOMIAL 1
+int vk_adjoint_set_schedule(vk_ctx* ctx, int32_t schedule);
 /* Autograd-Function backward: dJ/du_0 for the last vk_adjoint_forward, in the
  * L2 inner product of the physical fields (<a,b> = sum w Re(a conj b) / N^6),
  * projected onto real, divergence-free fields with zero Nyquist entries.
- * Segments are recomputed from their checkpoint storing u, a, b, c of every
- * step (4 ceil(nsteps/nsnap) + 1 states), then reversed. */
+ * Two-level schedule: segments are recomputed from their checkpoint storing
+ * u, a, b, c of every step (4 ceil(nsteps/nsnap) + 1 states), then reversed;
+ * binomial schedule: see vk_adjoint_set_schedule. */
 int vk_adjoint_backward(vk_ctx* ctx, double* gx, double* gy, double* gz);
 /* Transpose of compute_nonlinear's linearisation at x applied to nbar (raw
  * Euclidean inner product of the stored entries), on host arrays. */

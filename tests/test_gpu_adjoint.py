@@ -79,6 +79,23 @@ def test_checkpoint_schedule_does_not_change_gradient(vk):
             assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("nsnap", [1, 2, 3, 7])
+def test_binomial_schedule_gives_the_two_level_gradient(vk, nsnap):
+    # treeverse over nsnap slots (vk_adjoint_set_schedule) against the
+    # two-level schedule: the same steps in the same order, bitwise
+    n, nu, dt, nsteps = 16, 0.05, 0.02, 7
+    g, ops, u0 = state(n, 3)
+    out = {}
+    for sch in ("two-level", "binomial"):
+        s = vk.Periodic3D(vk.GridSpec(n), nu, u0, vk.SolverOptions(dt_mode="fixed", dt_fixed=dt))
+        J = s.adjoint_forward(nsteps, nsnap, schedule=sch)
+        out[sch] = (J, s.adjoint_backward())
+        s.close()
+    assert out["binomial"][0] == out["two-level"][0]
+    for a, b in zip(out["binomial"][1], out["two-level"][1]):
+        assert np.array_equal(a, b)
+
+
 def test_gradient_vs_central_fd_on_gpu(vk):
     from vonkarman_gb300 import ics
 

@@ -1,0 +1,41 @@
+"""Binomial checkpoint schedule (vonkarman_gb300/csrc/vk_schedule.h) on the
+CPU: a simulated executor whose states are step indices checks that every
+step is reversed exactly once, last first, from the right state; that no
+more than nsnap slots hold a state at once; and that the forward work stays
+within r sweeps of the chain (r the least with C(nsnap - 1 + r, r) >= nsteps)."""
+
+import math
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+CASES = [(1, 1), (2, 1), (7, 1), (10, 2), (20, 3), (100, 5), (1000, 20), (1000, 60), (997, 7), (64, 64),
+         (5000, 10)]
+
+
+@pytest.fixture(scope="module")
+def checker(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path_factory.mktemp("sched") / "schedule_check")
+    subprocess.run([cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "vonkarman_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "cpp", "schedule_check.cpp"), "-o", exe], check=True)
+    return exe
+
+
+def test_treeverse_reverses_every_step_within_slots_and_sweeps(checker):
+    args = [str(v) for case in CASES for v in case]
+    out = subprocess.run([checker, *args], check=True, capture_output=True, text=True).stdout.split("\n")
+    for (nsteps, nsnap), line in zip(CASES, out):
+        f = line.split()
+        assert f[0] == "ok", line
+        adv, slots, r = int(f[2]), int(f[3]), int(f[4])
+        assert slots <= nsnap
+        assert nsnap == 1 or math.comb(nsnap - 1 + r, r) >= nsteps
+        # every step is advanced at most r times in the reversal sweeps
+        assert adv <= r * nsteps, (nsteps, nsnap, adv, r)

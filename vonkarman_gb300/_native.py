@@ -71,6 +71,7 @@ SIGNATURES = {
     "vk_spectrum": (c_int, [_CTX, _DP, _DP, c_int32]),
     "vk_nonlinear_host": (c_int, [_CTX, _DP, _DP, _DP, _DP, _DP, _DP]),
     "vk_adjoint_forward": (c_int, [_CTX, c_int64, c_int32, _DP]),
+    "vk_adjoint_set_schedule": (c_int, [_CTX, c_int32]),
     "vk_adjoint_backward": (c_int, [_CTX, _DP, _DP, _DP]),
     "vk_nonlinear_adjoint_host": (c_int, [_CTX, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),
     "vk_step_timed": (c_int, [_CTX, c_int64, _DP]),

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "vk_host.h"
+#include "vk_schedule.h"
 #include "vonkarman_gpu.h"
 
 using vk::C2;
@@ -182,6 +183,8 @@ struct vk_ctx {
     size_t bufA_bytes = 0, bufB_bytes = 0;
     bool ready = false;
     double J = 0.0;
+    int schedule = VK_ADJ_TWO_LEVEL;   // for the next forward
+    int used = VK_ADJ_TWO_LEVEL;       // of the last forward
   } adj;
   cudaEvent_t tev[2] = {nullptr, nullptr};
   cudaEvent_t marks[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -875,6 +878,31 @@ cudaError_t forward_step_store(vk_ctx* c, void* S, void* A, void* B, void* C, vo
   return nle_stage(c, C, vk::ST_ETD_4, S, C, Snext);
 }
 
+// Device executor of the binomial schedule (vk_schedule.h): states live in
+// the checkpoint slots or the working buffer; advancing runs full steps in
+// place (the last stage's epilogue reads and writes u mode by mode).
+struct AdjBinomialEx {
+  vk_ctx* c;
+  void* work;
+  void* A;
+  void* B;
+  void* C;
+  size_t sb;
+  cudaError_t err = cudaSuccess;
+  void* buf(int s) const { return s < 0 ? work : c->adj.ckpt[(size_t)s]; }
+  bool ok() const { return err == cudaSuccess; }
+  void copy(int d, int s) {
+    if (ok()) err = cudaMemcpyAsync(buf(d), buf(s), sb, cudaMemcpyDeviceToDevice, c->stream);
+  }
+  void advance(int s, int64_t n) {
+    for (int64_t i = 0; i < n && ok(); ++i) err = forward_step_store(c, buf(s), A, B, C, buf(s));
+  }
+  void reverse_step(int s) {
+    if (ok()) err = forward_step_store(c, buf(s), A, B, C, nullptr);
+    if (ok()) err = adjoint_step(c, buf(s), A, B, C);
+  }
+};
+
 int adj_supported(vk_ctx* c) {
   if (!c->has_state) return fail(c, VK_ERR_STATE, "no state set");
   if (c->cfg.dt_mode != VK_DT_FIXED)
@@ -888,14 +916,24 @@ int adj_supported(vk_ctx* c) {
 
 extern "C" {
 
+int vk_adjoint_set_schedule(vk_ctx* c, int32_t schedule) {
+  if (!c) return VK_ERR_INVALID;
+  if (schedule != VK_ADJ_TWO_LEVEL && schedule != VK_ADJ_BINOMIAL)
+    return fail(c, VK_ERR_INVALID, "schedule must be VK_ADJ_TWO_LEVEL or VK_ADJ_BINOMIAL");
+  c->adj.schedule = schedule;
+  return VK_OK;
+}
+
 int vk_adjoint_forward(vk_ctx* c, int64_t nsteps, int32_t nsnap, double* J) {
   if (!c || !J) return VK_ERR_INVALID;
   int r = adj_supported(c);
   if (r != VK_OK) return r;
   if (nsteps < 1 || nsnap < 1) return fail(c, VK_ERR_INVALID, "nsteps >= 1 and nsnap >= 1 required");
   DeviceGuard g(c->cfg.device);
-  const int64_t K = (nsteps + nsnap - 1) / nsnap;
-  const int64_t nseg = (nsteps + K - 1) / K;
+  const bool binomial = c->adj.schedule == VK_ADJ_BINOMIAL;
+  // binomial: nsnap slots plus the working state and one step's stage inputs
+  const int64_t K = binomial ? 1 : (nsteps + nsnap - 1) / nsnap;
+  const int64_t nseg = binomial ? nsnap : (nsteps + K - 1) / K;
   cudaError_t e = adj_alloc(c, nseg, K);
   if (e != cudaSuccess) {
     free_adjoint(c);
@@ -904,11 +942,17 @@ int vk_adjoint_forward(vk_ctx* c, int64_t nsteps, int32_t nsnap, double* J) {
   auto& a = c->adj;
   a.nsteps = nsteps;
   a.ready = false;
+  a.used = binomial ? VK_ADJ_BINOMIAL : VK_ADJ_TWO_LEVEL;
   const size_t sb = state_bytes(c);
-  for (int64_t s = 0; s < nseg; ++s) {
-    VK_CHECK(c, cudaMemcpyAsync(a.ckpt[(size_t)s], c->u, sb, cudaMemcpyDeviceToDevice, c->stream));
-    const int64_t ks = std::min<int64_t>(K, nsteps - s * K);
-    for (int64_t j = 0; j < ks; ++j) VK_CHECK(c, step_once(c));
+  if (binomial) {
+    VK_CHECK(c, cudaMemcpyAsync(a.ckpt[0], c->u, sb, cudaMemcpyDeviceToDevice, c->stream));
+    for (int64_t j = 0; j < nsteps; ++j) VK_CHECK(c, step_once(c));
+  } else {
+    for (int64_t s = 0; s < nseg; ++s) {
+      VK_CHECK(c, cudaMemcpyAsync(a.ckpt[(size_t)s], c->u, sb, cudaMemcpyDeviceToDevice, c->stream));
+      const int64_t ks = std::min<int64_t>(K, nsteps - s * K);
+      for (int64_t j = 0; j < ks; ++j) VK_CHECK(c, step_once(c));
+    }
   }
   // J = enstrophy of the final state and its raw-Euclidean cotangent
   VK_CHECK(c, tier1_enqueue(c));
@@ -934,12 +978,22 @@ int vk_adjoint_backward(vk_ctx* c, double* gx, double* gy, double* gz) {
   void** B = A + K;
   void** C = B + K;
   const size_t sb = state_bytes(c);
-  for (int64_t s = a.nseg - 1; s >= 0; --s) {
-    const int64_t ks = std::min<int64_t>(K, a.nsteps - s * K);
-    VK_CHECK(c, cudaMemcpyAsync(S[0], a.ckpt[(size_t)s], sb, cudaMemcpyDeviceToDevice, c->stream));
-    for (int64_t j = 0; j < ks; ++j)
-      VK_CHECK(c, forward_step_store(c, S[j], A[j], B[j], C[j], j + 1 < ks ? S[j + 1] : nullptr));
-    for (int64_t j = ks - 1; j >= 0; --j) VK_CHECK(c, adjoint_step(c, S[j], A[j], B[j], C[j]));
+  if (a.used == VK_ADJ_BINOMIAL) {
+    // slots: the checkpoints (slot 0 = initial state), -1 = S[0]; one step's
+    // stage inputs in A[0], B[0], C[0]
+    AdjBinomialEx ex{c, S[0], A[0], B[0], C[0], sb};
+    std::vector<int> free_slots;
+    for (int k = (int)a.nseg - 1; k >= 1; --k) free_slots.push_back(k);
+    vk::treeverse(ex, 0, a.nsteps, 0, free_slots);
+    VK_CHECK(c, ex.err);
+  } else {
+    for (int64_t s = a.nseg - 1; s >= 0; --s) {
+      const int64_t ks = std::min<int64_t>(K, a.nsteps - s * K);
+      VK_CHECK(c, cudaMemcpyAsync(S[0], a.ckpt[(size_t)s], sb, cudaMemcpyDeviceToDevice, c->stream));
+      for (int64_t j = 0; j < ks; ++j)
+        VK_CHECK(c, forward_step_store(c, S[j], A[j], B[j], C[j], j + 1 < ks ? S[j + 1] : nullptr));
+      for (int64_t j = ks - 1; j >= 0; --j) VK_CHECK(c, adjoint_step(c, S[j], A[j], B[j], C[j]));
+    }
   }
   // gradient in the L2 inner product of the physical fields, projected on
   // real, divergence-free, Nyquist-free fields

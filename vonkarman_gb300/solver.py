@@ -220,9 +220,17 @@ class Periodic3D:
 
 
     # -- discrete adjoint (autograd-Function pattern) -------------------------
-    def adjoint_forward(self, nsteps: int, nsnap: int = 20) -> float:
+    ADJ_SCHEDULES = {"two-level": 0, "binomial": 1}
+
+    def adjoint_forward(self, nsteps: int, nsnap: int = 20, schedule: str = "two-level") -> float:
         """Run nsteps fixed-dt steps keeping nsnap checkpoints; returns
-        J = final enstrophy.  The state advances."""
+        J = final enstrophy.  The state advances.  schedule: "two-level"
+        (nsnap segment checkpoints, one recompute pass storing each segment's
+        stage inputs) or "binomial" (nsnap state slots reversed by the
+        treeverse schedule: less memory, more recomputation)."""
+        if schedule not in self.ADJ_SCHEDULES:
+            raise ValueError(f"schedule must be one of {sorted(self.ADJ_SCHEDULES)}")
+        self._call(self._lib.vk_adjoint_set_schedule, self.ADJ_SCHEDULES[schedule])
         v = ctypes.c_double()
         self._call(self._lib.vk_adjoint_forward, int(nsteps), int(nsnap), ctypes.byref(v))
         return v.value

@@ -23,10 +23,11 @@ def _axpy(a, x, y):
     return [a * xi + yi for xi, yi in zip(x, y)]
 
 
-def gradient(solver: Periodic3D, u0, nsteps: int, nsnap: int = 20):
-    """J(u0) and dJ/du0 with the solver's configuration (fixed dt)."""
+def gradient(solver: Periodic3D, u0, nsteps: int, nsnap: int = 20, schedule: str = "two-level"):
+    """J(u0) and dJ/du0 with the solver's configuration (fixed dt); schedule
+    is the checkpoint schedule of the adjoint ("two-level" or "binomial")."""
     solver.restore_state(u0, 0.0, 0, solver.options.dt_fixed)
-    J = solver.adjoint_forward(nsteps, nsnap)
+    J = solver.adjoint_forward(nsteps, nsnap, schedule=schedule)
     return J, solver.adjoint_backward()
 
 

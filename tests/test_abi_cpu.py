@@ -101,3 +101,6 @@ def test_null_arguments(lib):
     assert lib.vk_step(None, 1) == 1
     assert lib.vk_destroy(None) == 0
     assert lib.vk_spectral_len(None) == -1
+    assert lib.vk_adjoint_set_schedule(None, 0) == 1
+    assert lib.vk_adjoint_forward(None, 10, 2, None) == 1
+    assert lib.vk_adjoint_backward(None, None, None, None) == 1

@@ -1,18 +1,22 @@
-// Register-resident batched line FFT for the strided (x / y) passes.
+// Register-resident batched line FFT and the pass kernels built on it
+// (k_lines: strided x / y passes; k_p5: x-forward with the stage epilogue;
+// k_p3: the z pass with the cross product; k_nz_max: the N-grid z pass).
 //
-// NLINES interleaved lines of length L are transformed by a Stockham
-// auto-sort whose stages live in registers: the first stage reads its
-// butterfly inputs straight from global memory (through the pass's load
-// functor, which also applies zero-padding and derivative factors), every
+// NLINES lines of length L are transformed by a Stockham auto-sort whose
+// stages live in registers: the first stage reads its butterfly inputs
+// straight from global memory (through the pass's load functor, which also
+// applies zero-padding and derivative factors; inputs that are padding for
+// every butterfly are compile-time zeros whose additions are skipped), every
 // later stage reads them from a shared-memory exchange buffer written by the
 // stage before, and the last stage hands its outputs straight to the pass's
 // store functor (which applies truncation).  With the FP32 plans (two stages
 // for every padded length up to 768) each element crosses shared memory once.
 //
-// Thread g handles butterfly j = g / NLINES of line l = g % NLINES in every
-// stage, so consecutive lanes take consecutive lines: with the lines
-// consecutive in memory (z fastest) global accesses are row segments of
-// NLINES elements.
+// Thread-to-butterfly maps: interleaved lines (x / y passes, MapInterleaved):
+// thread g handles butterfly j = g / NLINES of line l = g % NLINES, so
+// consecutive lanes take consecutive lines and global accesses are row
+// segments of NLINES elements; contiguous lines (z passes, MapContig):
+// consecutive lanes take consecutive butterflies of one line.
 #pragma once
 
 #include <type_traits>

@@ -43,7 +43,9 @@ def run_to_time(solver: Periodic3D, t_end: float, every: int = 1, max_chunk: int
     """Step until ``solver.time() >= t_end`` (the stop rule of run.rs:152-155)
     and return the Tier-1 records of every ``every``-th step.  Chunks are sized
     from the current dt so that the loop does not pass the first step that
-    reaches ``t_end``; the last few steps are taken one at a time."""
+    reaches ``t_end``; the last few steps are taken one at a time (with
+    ``every`` > 1 chunks are multiples of ``every``, so the run may end up to
+    ``every`` - 1 steps past that step)."""
     recs = []
     while solver.time() < t_end:
         dt = solver.dt()

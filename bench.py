@@ -492,7 +492,10 @@ def run_ours(args, d: Dist):
                      "frac": achieved / hbm, "traffic": scaled_traffic(dom, args.precision, n),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (FP64: N=128 scaled by M^2 H; FP32-bulk: N=256)",
                      "peak_source": hbm_src,
-                     "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
+                     "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms,
+                     "note": ("HBM fraction of the FP64 form's dominant kernel, which is bound by the FP64 pipe "
+                              "(86 % of its cycles active in ncu): see fp64_roofline")
+                     if args.precision == "fp64" else "FP32-bulk: bound by the L1/shared-memory pipe (ncu)"},
         "fp64_roofline": {"kernel": dom, "achieved": dom_gflops, "peak": fp64_peak, "unit": "GFLOP/s",
                           "frac": dom_gflops / fp64_peak, "peak_source": "measured live (FP64 FMA probe)",
                           "note": "the FP64 form is bound by GB300's FP64 pipe, not HBM"}

@@ -495,7 +495,9 @@ def run_ours(args, d: Dist):
                      "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms,
                      "note": ("HBM fraction of the FP64 form's dominant kernel, which is bound by the FP64 pipe "
                               "(86 % of its cycles active in ncu): see fp64_roofline")
-                     if args.precision == "fp64" else "FP32-bulk: bound by the L1/shared-memory pipe (ncu)"},
+                     if args.precision == "fp64" else
+                     ("FP32-bulk P3: bound by the L1/shared-memory pipe (82 % in ncu at N=256)"
+                      if dom == "P3_z_c2r_cross_r2c" else None)},
         "fp64_roofline": {"kernel": dom, "achieved": dom_gflops, "peak": fp64_peak, "unit": "GFLOP/s",
                           "frac": dom_gflops / fp64_peak, "peak_source": "measured live (FP64 FMA probe)",
                           "note": "the FP64 form is bound by GB300's FP64 pipe, not HBM"}

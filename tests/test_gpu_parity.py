@@ -360,6 +360,21 @@ def test_run_records_match_tier1(vk):
             assert getattr(r, k) == getattr(t, k), k
 
 
+@pytest.mark.parametrize("integrator,variant", [("rk4", "reference"), ("etd-rk4", "cox-matthews")])
+def test_fp32bulk_one_step_other_integrators(vk, integrator, variant):
+    # the RK4 and Cox-Matthews stage epilogues in the FP32-bulk form
+    n = 32
+    g = vo.Grid(n)
+    u0 = vo.hermitian_clean(g, vo.random_field(g, 4, amp=100.0))
+    ref = vo.Periodic3D(g, 0.01, u0, dt_mode="fixed", dt_fixed=2e-3, integrator=integrator, etd_variant=variant)
+    ref.step()
+    s = vk.Periodic3D(vk.GridSpec(n), 0.01, u0, vk.SolverOptions(precision="fp32bulk", dt_mode="fixed",
+                                                                   dt_fixed=2e-3, integrator=integrator,
+                                                                   etd_variant=variant))
+    s.step()
+    assert nrel(s.u_hat(), ref.u_hat) < TOL32
+
+
 def test_fp32bulk_one_step(vk):
     n = 32
     g = vo.Grid(n)

@@ -10,11 +10,15 @@ shell spectrum E(k) every 10 steps.  Inputs are synthetic (seeded).
 
 Our arm prints one JSON line with the FP64 form as the headline (`value`,
 steps/s over all ranks), the FP32-bulk form beside it, the roofline of the
-dominant kernel, the end-to-end rate through the C ABI with host buffers, and
-the CPU restatement timed on this host.  The reference arm (`--impl
+dominant kernel, the end-to-end rate through the C ABI with host buffers, the
+CPU restatement timed on this host, the reference's cuFFT GPU mode (its
+stepper with per-call host <-> device copies around cuFFT), the N=512
+vortex-tube target workload in both forms, and the checkpointed adjoint
+(binomial and two-level schedules, 1000 steps).  The reference arm (`--impl
 reference`) times the CPU restatement of the reference's path with all host
-threads on the same workload.  Multi-GPU: the path does not shard on one box
-(replicas only), so N ranks run N independent replicas.
+threads on the same workload, exactly --warmup + --steps steps, plus one step
+on one thread.  Multi-GPU: the path does not shard on one box (replicas
+only), so N ranks run N independent replicas.
 """
 
 from __future__ import annotations
@@ -55,8 +59,14 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--adjoint-steps", type=int, default=100,
+    ap.add_argument("--adjoint-steps", type=int, default=1000,
                     help="steps of the checkpointed adjoint measurement (0 = skip)")
+    ap.add_argument("--adjoint-schedule", choices=["binomial", "two-level", "both"], default="both",
+                    help="checkpoint schedule(s) of the adjoint measurement")
+    ap.add_argument("--tubes-steps", type=int, default=20,
+                    help="steps of each form in the N=512 vortex-tube leg (0 = skip)")
+    ap.add_argument("--no-cufft-baseline", action="store_true",
+                    help="skip the reference's cuFFT GPU-mode baseline leg")
     ap.add_argument("--precision", choices=["fp64", "fp32bulk"], default="fp64",
                     help="form of the headline run (fp32bulk only for profiling that form)")
     return ap.parse_args()
@@ -241,27 +251,49 @@ def host_cores() -> int:
 
 
 def run_reference(args, d: Dist):
+    """The reference's CPU path (C restatement, oracle/vk_cpu.c) on this host's
+    cores: exactly --warmup untimed and --steps timed ETD-RK4 steps of the
+    benchmark workload, with E(k) after every --spectrum-every-th step as in
+    our arm, then one step on a single thread (the reference itself is
+    serial)."""
     if d.rank != 0:
         return
+    from oracle import vk_cpu
     from vonkarman_gb300 import ics
 
     n, nu = args.n, 1e-3
     u0 = ics.von_karman_isotropic(n, kp=4.0, energy=0.5, seed=42)
     cores = host_cores()
-    # bounded sample: a full CPU step at N=256 takes tens of seconds, so at most
-    # 3 timed steps after at most 1 warm-up step keep the run within minutes
-    ksteps = max(1, min(args.steps, 3))
-    kwarm = min(args.warmup, 1)
-    el = time_cpu(u0, n, nu, kwarm, ksteps, cores)
-    v = ksteps / el
+    vk_cpu.set_threads(cores)
+    s = vk_cpu.CpuSolver(n, nu, u0)
+    for i in range(args.warmup):
+        s.step(1)
+    t0 = time.perf_counter()
+    for i in range(1, args.steps + 1):
+        s.step(1)
+        if args.spectrum_every > 0 and i % args.spectrum_every == 0:
+            s.spectrum()
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    # single thread: one more step of the same run
+    vk_cpu.set_threads(1)
+    t1 = time.perf_counter()
+    s.step(1)
+    el1 = time.perf_counter() - t1
+    vk_cpu.set_threads(cores)
+    s.close()
+    sample = (f"{args.steps} full ETD-RK4 steps (CFL pass, ETD re-tabulation when dt moves > 1 %, E(k) every "
+              f"{args.spectrum_every} steps) after {args.warmup} warm-up steps, C restatement of the reference's "
+              f"CPU path (oracle/vk_cpu.c), OpenMP on {cores} threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / ksteps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "n": n, "precision": "fp64", "replicas": 1},
-        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{ksteps} full ETD-RK4 steps after {kwarm} warm-up step(s), "
-                                   f"C restatement of the reference's CPU path (oracle/vk_cpu.c), OpenMP"},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "single_thread": {"value": 1.0 / el1, "unit": "steps/s", "cores": 1, "kind": "port",
+                          "sample": "1 full ETD-RK4 step of the same run on one thread (the reference's own "
+                                    "schedule: its CPU path is serial)"},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -301,15 +333,17 @@ def timed_run(s, steps: int, spec_every: int):
 
 def measure_adjoint(args, grid, dev, d: Dist):
     """Checkpointed discrete adjoint on the checkpointed-ascent workload:
-    random isotropic start (kp=3, E=0.5), nu=2e-3, fixed dt=1e-3, 20 level-1
-    checkpoints, FP32-bulk; cost relative to a plain forward run of the same
-    steps, and the FP32-bulk gradient against the FP64 one on a shorter run."""
+    random isotropic start (kp=3, E=0.5), nu=2e-3, fixed dt=1e-3, 20 saved
+    states, FP32-bulk.  Per schedule: (checkpointed forward + backward) cost
+    relative to a plain forward run of the same steps, and the states the
+    schedule holds.  The FP32-bulk gradient is checked against the FP64 one on
+    a 20-step run."""
     import vonkarman_gb300 as vk
     from vonkarman_gb300 import ics
 
     n, nu, dt = grid.n, 2e-3, 1e-3
     u0 = ics.project_control(ics.von_karman_isotropic(n, kp=3.0, energy=0.5, seed=42), n)
-    k = args.adjoint_steps
+    k, nsnap = args.adjoint_steps, 20
     opts = vk.SolverOptions(precision="fp32bulk", dt_mode="fixed", dt_fixed=dt, device=dev)
     s = vk.Periodic3D(grid, nu, u0, opts)
     s.step(2)
@@ -318,30 +352,146 @@ def measure_adjoint(args, grid, dev, d: Dist):
     s.step(k)
     s.event_mark(1)
     fwd_ms = d.max(s.event_elapsed(0, 1))
-    s.restore_state(u0, 0.0, 0, dt)
-    s.event_mark(2)
-    s.adjoint_forward(k, 20)
-    s.event_mark(3)
-    g32 = s.adjoint_backward()
-    s.event_mark(4)
-    af_ms = d.max(s.event_elapsed(2, 3))
-    ab_ms = d.max(s.event_elapsed(3, 4))
     s.close()
+    state_gb = 3 * n * n * (n // 2 + 1) * 8 / 1e9
+    scheds = ["binomial", "two-level"] if args.adjoint_schedule == "both" else [args.adjoint_schedule]
+    out = {"workload": f"random isotropic kp=3 E=0.5, N={n}, nu=2e-3, fixed dt=1e-3, {k} steps, "
+                       f"{nsnap} saved states, FP32-bulk",
+           "forward_ms": fwd_ms, "schedules": {}}
+    for sch in scheds:
+        s = vk.Periodic3D(grid, nu, u0, opts)
+        s.event_mark(2)
+        s.adjoint_forward(k, nsnap, schedule=sch)
+        s.event_mark(3)
+        s.adjoint_backward()
+        s.event_mark(4)
+        af_ms = d.max(s.event_elapsed(2, 3))
+        ab_ms = d.max(s.event_elapsed(3, 4))
+        s.close()
+        seg = -(-k // nsnap)
+        states = nsnap + 5 + 4 if sch == "binomial" else nsnap + 4 * seg + 1 + 4
+        out["schedules"][sch] = {
+            "adjoint_forward_ms": af_ms, "adjoint_backward_ms": ab_ms, "total_over_forward": (af_ms + ab_ms) / fwd_ms,
+            "states_held": states, "state_memory_gb": states * state_gb,
+            "layout": ("20 state slots reversed by the binomial (treeverse) schedule" if sch == "binomial" else
+                       f"20 level-1 checkpoints, each {seg}-step segment recomputed once storing its stage inputs")}
     # FP32-bulk vs FP64 gradient on 20 steps
     kk = min(20, k)
     grads = []
     for prec in ("fp64", "fp32bulk"):
         t = vk.Periodic3D(grid, nu, u0, vk.SolverOptions(precision=prec, dt_mode="fixed", dt_fixed=dt, device=dev))
-        t.adjoint_forward(kk, 20)
+        t.adjoint_forward(kk, nsnap, schedule=scheds[0])
         grads.append(t.adjoint_backward())
         t.close()
-    num = math.sqrt(sum(float(np.sum(np.abs(a - b) ** 2)) for a, b in zip(grads[1], grads[0])))
-    den = math.sqrt(sum(float(np.sum(np.abs(b) ** 2)) for b in grads[0]))
-    return {"workload": f"random isotropic kp=3 E=0.5, N={n}, nu=2e-3, fixed dt=1e-3, {k} steps, "
-                        "20 level-1 checkpoints, FP32-bulk",
-            "forward_ms": fwd_ms, "adjoint_forward_ms": af_ms, "adjoint_backward_ms": ab_ms,
-            "backward_over_forward": ab_ms / fwd_ms, "total_over_forward": (af_ms + ab_ms) / fwd_ms,
-            "fp32_vs_fp64_gradient_rel_l2": num / den, "gradient_check_steps": kk}
+    diff = [a - b for a, b in zip(grads[1], grads[0])]
+    out["fp32_vs_fp64_gradient_rel_l2"] = math.sqrt(vk.l2_inner(diff, diff, n) / vk.l2_inner(grads[0], grads[0], n))
+    out["gradient_check_steps"] = kk
+    return out
+
+
+def profile_passes(s, steps: int, n: int, elem: int, hbm: float):
+    """Per-pass CUDA-event timing of `steps` steps: ms per launch, launches and
+    the algorithmic GB/s of each pass of the byte model against the measured
+    HBM copy bandwidth."""
+    s.profile(True)
+    s.step(steps)
+    prof = s.profile_read()
+    s.profile(False)
+    mdl = pass_model(n)
+    tot = sum(t for t, c in prof.values())
+    passes = {}
+    for k, (t, c) in prof.items():
+        if not c:
+            continue
+        e = {"ms_per_launch": t / c, "launches": c, "share": t / tot if tot else None}
+        if k in mdl:
+            gbs = mdl[k][0] * elem / (t / c * 1e-3) / 1e9
+            e["gbs"] = gbs
+            e["hbm_frac"] = gbs / hbm
+        passes[k] = e
+    return prof, passes
+
+
+def measure_tubes(args, dev, d: Dist):
+    """The target workload: anti-parallel Lamb-Oseen tubes at N=512 (768^3
+    padded), nu=5e-4, adaptive CFL 0.5, Tier-1 (max|omega|, enstrophy, ...)
+    after every step, in both forms from the same initial state: steps/s,
+    per-pass GB/s, and the FP32-bulk form's error against the FP64 GPU run
+    after the same steps (E, enstrophy, max|omega|, per-shell E(k))."""
+    import vonkarman_gb300 as vk
+    from vonkarman_gb300 import ics
+
+    n, nu, k = 512, 5e-4, args.tubes_steps
+    u0 = ics.lamb_oseen_tubes(n)
+    hbm, _ = measured_hbm()
+    out = {"workload": f"anti-parallel Lamb-Oseen tubes N={n} (768^3 padded), Gamma=+-1, sigma=0.25, d=1, "
+                       f"x-displacement 0.1 sin z, nu={nu}, adaptive CFL 0.5, Tier-1 after every step; "
+                       f"{k} timed steps per form after 2 warm-up steps", "forms": {}}
+    finals = {}
+    for prec, elem in (("fp64", 16), ("fp32bulk", 8)):
+        s = vk.Periodic3D(vk.GridSpec(n), nu, u0, vk.SolverOptions(precision=prec, device=dev))
+        s.run(2, every=1)
+        d.barrier()
+        s.event_mark(0)
+        recs = s.run(k, every=1)
+        s.event_mark(1)
+        ms = d.max(s.event_elapsed(0, 1))
+        _, spec = vk.energy_spectrum(s)
+        finals[prec] = (recs[-1], spec)
+        prof, passes = profile_passes(s, 1, n, elem, hbm)
+        mdl = pass_model(n)
+        dom = max((p for p in mdl if prof.get(p, (0, 0))[1] > 0), key=lambda p: prof[p][0])
+        out["forms"][prec] = {"steps_per_s": d.world * k / (ms / 1e3), "ms_per_step": ms / k,
+                              "hbm_gbs_step": step_bytes(n, elem) / (ms / k * 1e-3) / 1e9,
+                              "time_reached": recs[-1].time, "step": recs[-1].step,
+                              "dominant_kernel": dom, "passes": passes}
+        s.close()
+    f64, f32 = out["forms"]["fp64"], out["forms"]["fp32bulk"]
+    out["speedup_fp32bulk_over_fp64"] = f32["steps_per_s"] / f64["steps_per_s"]
+    (a, sa), (b, sb) = finals["fp64"], finals["fp32bulk"]
+    rel = lambda x, y: abs(x - y) / max(abs(y), 1e-300)  # noqa: E731
+    keep = sa > 1e-12 * sa.max()
+    out["fp32bulk_error_vs_fp64_gpu"] = {
+        "after_steps": int(a.step), "time_fp64": a.time, "time_fp32bulk": b.time,
+        "energy": rel(b.energy, a.energy), "enstrophy": rel(b.enstrophy, a.enstrophy),
+        "max_vorticity": rel(b.max_vorticity, a.max_vorticity),
+        "spectrum_max_rel_shell": float(np.max(np.abs(sb - sa)[keep] / sa[keep])),
+        "spectrum_max_abs_over_max": float(np.max(np.abs(sb - sa)) / sa.max())}
+    return out
+
+
+def measure_cufft_mode(n: int, nu: float, u0, steps: int = 2):
+    """The reference's own GPU mode (BackendMode::Cufft, vonkarman-fft/src/select.rs:34-67):
+    its CPU stepper with every 3-D transform sent through cuFFT with a
+    host -> device copy, cufftExecD2Z / Z2D and a device -> host copy per call
+    and the 1/N^3 on the host (vonkarman-fft/src/cufft.rs:249-319), restated in
+    oracle/vk_cpu.c.  Baseline leg only: cuFFT is not on this library's path."""
+    from oracle import vk_cpu
+
+    try:
+        vk_cpu.set_cufft(True)
+    except RuntimeError as e:
+        return {"unavailable": str(e)}
+    cores = host_cores()
+    vk_cpu.set_threads(cores)
+    try:
+        c = vk_cpu.CpuSolver(n, nu, u0)
+        if not c.uses_cufft():
+            c.close()
+            return {"unavailable": "cuFFT plan or device buffer set-up failed"}
+        c.step(1)
+        t0 = time.perf_counter()
+        c.step(steps)
+        el = time.perf_counter() - t0
+        c.close()
+    finally:
+        vk_cpu.set_cufft(False)
+    return {"value": steps / el, "unit": "steps/s", "ms_per_step": 1e3 * el / steps, "cores": cores,
+            "kind": "port",
+            "sample": f"{steps} full ETD-RK4 steps after 1 warm-up step: the C restatement of the reference's "
+                      f"stepper with the reference's cuFFT backend pattern (45 3-D transforms per step, each "
+                      f"cudaMemcpy H2D + cufftExecD2Z/Z2D + cudaMemcpy D2H, host 1/N^3), pageable host arrays, "
+                      f"CPU parts on {cores} threads"}
 
 
 def run_ours(args, d: Dist):
@@ -367,28 +517,20 @@ def run_ours(args, d: Dist):
     value = d.world * args.steps / (ms / 1e3)
 
     # per-pass profile (separate run, events around every launch)
-    s.profile(True)
+    hbm, hbm_src = measured_hbm()
     prof_steps = 2
-    s.step(prof_steps)
-    prof = s.profile_read()
-    s.profile(False)
+    elem = 16 if args.precision == "fp64" else 8
+    prof, passes = profile_passes(s, prof_steps, n, elem, hbm)
     launches_per_step = sum(c for k, (t, c) in prof.items() if k not in ("spectrum", "tier1_sums")) / prof_steps
     gpu_launches = int(round(launches_per_step * args.steps)) + 2 * nspec
 
     mdl = pass_model(n)
-    elem = 16 if args.precision == "fp64" else 8
     dom = max((k for k in mdl if prof.get(k, (0, 0))[1] > 0), key=lambda k: prof[k][0])
     dom_ms = prof[dom][0] / prof[dom][1]
-    hbm, hbm_src = measured_hbm()
     dom_bytes = mdl[dom][0] * elem
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     fp64_peak = probe_fma_peak(dev, True)
     dom_gflops = mdl[dom][1] / (dom_ms * 1e-3) / 1e9
-    passes = {k: {"ms_per_launch": (t / c if c else None), "launches": c, "share": None}
-              for k, (t, c) in prof.items() if c}
-    tot = sum(t for t, c in prof.values())
-    for k in passes:
-        passes[k]["share"] = prof[k][0] / tot if tot else None
     sb = step_bytes(n, elem)
     fp64_res = {}
     if d.rank == 0:
@@ -438,10 +580,7 @@ def run_ours(args, d: Dist):
         d.barrier()
         ms32, _ = timed_run(s32, args.steps, args.spectrum_every)
         ms32 = d.max(ms32)
-        s32.profile(True)
-        s32.step(prof_steps)
-        prof32 = s32.profile_read()
-        s32.profile(False)
+        prof32, passes32 = profile_passes(s32, prof_steps, n, 8, hbm)
         dom32 = max((k for k in mdl if prof32.get(k, (0, 0))[1] > 0), key=lambda k: prof32[k][0])
         d32_ms = prof32[dom32][0] / prof32[dom32][1]
         fp32 = {"steps_per_s": d.world * args.steps / (ms32 / 1e3), "ms_per_step": ms32 / args.steps,
@@ -449,7 +588,9 @@ def run_ours(args, d: Dist):
                 "dominant_kernel": dom32,
                 "dominant_roofline": {"bound": "hbm", "achieved": mdl[dom32][0] * 8 / (d32_ms * 1e-3) / 1e9,
                                       "peak": hbm, "unit": "GB/s",
-                                      "frac": mdl[dom32][0] * 8 / (d32_ms * 1e-3) / 1e9 / hbm}}
+                                      "frac": mdl[dom32][0] * 8 / (d32_ms * 1e-3) / 1e9 / hbm,
+                                      "traffic": scaled_traffic(dom32, "fp32bulk", n)},
+                "passes": passes32}
         if d.rank == 0 and fp64_res:
             t32 = s32.tier1()
             _, spec32 = vk.energy_spectrum(s32)
@@ -469,6 +610,14 @@ def run_ours(args, d: Dist):
     adjoint = None
     if args.adjoint_steps > 0 and args.precision == "fp64":
         adjoint = measure_adjoint(args, grid, dev, d)
+
+    tubes = None
+    if args.tubes_steps > 0 and args.precision == "fp64":
+        tubes = measure_tubes(args, dev, d)
+
+    cufft_mode = None
+    if d.rank == 0 and d.world == 1 and not args.no_cufft_baseline:
+        cufft_mode = measure_cufft_mode(n, nu, u0)
 
     cpu = None
     if d.rank == 0 and d.world == 1 and not args.no_cpu_baseline:
@@ -509,6 +658,8 @@ def run_ours(args, d: Dist):
         "clocks": clocks,
         "fp32bulk": fp32,
         "adjoint": adjoint,
+        "tubes_n512": tubes,
+        "reference_cufft_mode": cufft_mode,
         "sps_per_rank": sps_rank,
     }
     print(json.dumps(line), flush=True)

@@ -15,7 +15,13 @@
  * aborts; vk_last_error() returns the message of the last failure on that
  * context (or of the last failed vk_create / vk_fft_create when ctx is NULL).
  * The reference panics on CUDA execution errors (vonkarman-fft/src/cufft.rs:262-314);
- * this boundary reports them instead.
+ * this boundary reports them instead.  A NaN or infinity that enters the
+ * solver state (seen by a CFL / max pass, or written by the final stage of a
+ * step) makes the next call that synchronises -- vk_time, vk_dt, vk_cfl_dt,
+ * vk_tier1 and its field getters, vk_run, vk_step_timed -- return
+ * VK_ERR_NONFINITE, the NaN check of the reference's audit
+ * (vonkarman-diag/src/audit.rs:175-197); vk_step itself enqueues without a
+ * readback.  Setting a new state clears the condition.
  *
  * Threading.  One context per thread; each context owns one CUDA stream and
  * keeps its solver state resident in device memory.  Calls are synchronous
@@ -165,6 +171,18 @@ int vk_spectrum(vk_ctx* ctx, double* shells, double* spectrum, int32_t n);
 int vk_nonlinear_host(vk_ctx* ctx, const double* ux, const double* uy, const double* uz, double* nx_out,
                       double* ny_out, double* nz_out);
 
+/* SpectralOps::apply_viscous (vonkarman-core/src/spectral_ops.rs:154-175) on
+ * host arrays: out_c = -(nu |k|^2) u_c, |k|^2 formed as SpectralOps::new does
+ * (spectral_ops.rs:26-44); computed on the device in the context's precision,
+ * does not touch the solver state. */
+int vk_apply_viscous_host(vk_ctx* ctx, double nu, const double* ux, const double* uy, const double* uz,
+                          double* out_x, double* out_y, double* out_z);
+/* The public fields of SpectralOps (spectral_ops.rs:10-22): kx, ky (n
+ * entries, index n/2 mapped to -n/2), kz (n/2+1 entries) and, unless NULL,
+ * k_mag_sq ((n, n, n/2+1) doubles, C order), bit-identical to
+ * SpectralOps::new (spectral_ops.rs:26-74). */
+int vk_wavenumbers(vk_ctx* ctx, double* kx, double* ky, double* kz, double* k_mag_sq);
+
 /* --- discrete adjoint (no reference counterpart: the reference has no
  *     adjoint; the forward map it differentiates is Domain::step with the
  *     reference ETD-RK4 stages, solver.rs:221-400) --------------------------- */
@@ -238,7 +256,11 @@ int vk_pinned_free(void* p);
  *   stream       cudaStream_t to enqueue on (NULL = default stream); the call
  *                returns without synchronising.
  * The first call on each device looks up the scratch address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * (cudaGetSymbolAddress, which also loads the module); make that first call
+ * before any stream capture.  The address is looked up again when the
+ * device's context changes (after a device reset).  The sums are the
+ * Neumaier-compensated column sums of vk_spectrum over 256 partial blocks
+ * (vk_spectrum: 8 per SM), so the two agree to rounding, not bitwise.
  * All calls share the one scratch array: calls that overlap on the GPU (other
  * streams, concurrently launched graphs) race and must be serialised by the
  * caller.  Errors: VK_ERR_INVALID / VK_ERR_UNSUPPORTED (n > 512), message in

@@ -24,7 +24,7 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
             os.path.getmtime(SRC), os.path.getmtime(os.path.abspath(__file__))):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
-    cmd = ["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-o", LIB + ".tmp", SRC, "-lm"]
+    cmd = ["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-o", LIB + ".tmp", SRC, "-lm", "-ldl"]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

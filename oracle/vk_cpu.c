@@ -24,9 +24,14 @@
  * precomputed twiddles; real transforms use the half-length complex trick
  * (the method of realfft, which ndrustfft calls).  OpenMP parallelises over
  * lanes and modes; with one thread it is the reference's serial schedule.
+ * vkc_set_cufft(1) switches the 3-D transforms to the reference's cuFFT
+ * backend pattern (per-call host <-> device copies around cuFFT, host-side
+ * normalisation: vonkarman-fft/src/cufft.rs), the reference's GPU mode.
  */
+#include <dlfcn.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -181,16 +186,128 @@ typedef struct {
   int nx, ny, nz, hz;
   fft1d fx, fy;
   rfft1d fz;
+  /* cuFFT mode (vkc_set_cufft): device buffers and D2Z / Z2D plans made once
+   * per backend, as CufftBackend::new does (vonkarman-fft/src/cufft.rs:193-241) */
+  int cufft;
+  void* d_real;
+  void* d_cplx;
+  int plan_d2z, plan_z2d;
 } backend;
+
+/* ------------------------------------------------------------------------- */
+/* cuFFT mode: the reference's GPU backend (vonkarman-fft/src/cufft.rs),       */
+/* restated.  libcudart / libcufft are loaded at run time (cufft.rs:76-168);   */
+/* every transform copies its input host -> device with a blocking cudaMemcpy, */
+/* runs cufftExecD2Z / Z2D and copies the result back (cufft.rs:249-319); c2r  */
+/* divides by nx ny nz on the host afterwards (cufft.rs:317-318).  Only the    */
+/* timed baseline of the reference's GPU mode uses it.                         */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  int loaded;
+  void* cudart;
+  void* cufft;
+  int (*cuda_malloc)(void**, size_t);
+  int (*cuda_free)(void*);
+  int (*cuda_memcpy)(void*, const void*, size_t, int);
+  int (*plan_3d)(int*, int, int, int, int);
+  int (*exec_d2z)(int, double*, void*);
+  int (*exec_z2d)(int, void*, double*);
+  int (*destroy)(int);
+} cuda_libs;
+
+static cuda_libs g_cu;
+static int g_use_cufft = 0;
+static char g_cu_err[256] = "";
+enum { CUFFT_D2Z_ = 0x6a, CUFFT_Z2D_ = 0x6c, MEMCPY_H2D_ = 1, MEMCPY_D2H_ = 2 };
+
+static void* open_first(const char* const* names) {
+  for (int i = 0; names[i]; ++i) {
+    void* h = dlopen(names[i], RTLD_NOW | RTLD_LOCAL);
+    if (h) return h;
+  }
+  return NULL;
+}
+
+static int cu_load(void) {
+  if (g_cu.loaded) return 0;
+  static const char* const rt[] = {"libcudart.so", "libcudart.so.13", "libcudart.so.12",
+                                   "/usr/local/cuda/lib64/libcudart.so", NULL};
+  static const char* const ff[] = {"libcufft.so", "libcufft.so.12", "libcufft.so.11",
+                                   "/usr/local/cuda/lib64/libcufft.so", NULL};
+  g_cu.cudart = open_first(rt);
+  g_cu.cufft = open_first(ff);
+  if (!g_cu.cudart || !g_cu.cufft) {
+    snprintf(g_cu_err, sizeof g_cu_err, "cannot load %s", g_cu.cudart ? "libcufft.so" : "libcudart.so");
+    return 1;
+  }
+  *(void**)&g_cu.cuda_malloc = dlsym(g_cu.cudart, "cudaMalloc");
+  *(void**)&g_cu.cuda_free = dlsym(g_cu.cudart, "cudaFree");
+  *(void**)&g_cu.cuda_memcpy = dlsym(g_cu.cudart, "cudaMemcpy");
+  *(void**)&g_cu.plan_3d = dlsym(g_cu.cufft, "cufftPlan3d");
+  *(void**)&g_cu.exec_d2z = dlsym(g_cu.cufft, "cufftExecD2Z");
+  *(void**)&g_cu.exec_z2d = dlsym(g_cu.cufft, "cufftExecZ2D");
+  *(void**)&g_cu.destroy = dlsym(g_cu.cufft, "cufftDestroy");
+  if (!g_cu.cuda_malloc || !g_cu.cuda_free || !g_cu.cuda_memcpy || !g_cu.plan_3d || !g_cu.exec_d2z ||
+      !g_cu.exec_z2d || !g_cu.destroy) {
+    snprintf(g_cu_err, sizeof g_cu_err, "missing cudart / cufft symbols");
+    return 1;
+  }
+  g_cu.loaded = 1;
+  return 0;
+}
+
+static int cufft_backend_init(backend* b) {
+  const size_t nreal = (size_t)b->nx * b->ny * b->nz, ncplx = (size_t)b->nx * b->ny * b->hz;
+  int rc = g_cu.cuda_malloc(&b->d_real, nreal * sizeof(double));
+  if (rc == 0) rc = g_cu.cuda_malloc(&b->d_cplx, ncplx * 2 * sizeof(double));
+  if (rc == 0) rc = g_cu.plan_3d(&b->plan_d2z, b->nx, b->ny, b->nz, CUFFT_D2Z_);
+  if (rc == 0) rc = g_cu.plan_3d(&b->plan_z2d, b->nx, b->ny, b->nz, CUFFT_Z2D_);
+  if (rc != 0) snprintf(g_cu_err, sizeof g_cu_err, "cuFFT backend set-up failed (code %d)", rc);
+  b->cufft = rc == 0;
+  return rc;
+}
 
 static void backend_init(backend* b, int nx, int ny, int nz) {
   b->nx = nx; b->ny = ny; b->nz = nz; b->hz = nz / 2 + 1;
   fft1d_init(&b->fx, nx);
   fft1d_init(&b->fy, ny);
   rfft1d_init(&b->fz, nz);
+  b->cufft = 0;
+  b->d_real = b->d_cplx = NULL;
+  b->plan_d2z = b->plan_z2d = 0;
+  if (g_use_cufft) cufft_backend_init(b);
 }
 
-static void backend_free(backend* b) { fft1d_free(&b->fx); fft1d_free(&b->fy); rfft1d_free(&b->fz); }
+static void backend_free(backend* b) {
+  fft1d_free(&b->fx); fft1d_free(&b->fy); rfft1d_free(&b->fz);
+  if (b->cufft) {
+    g_cu.destroy(b->plan_d2z);
+    g_cu.destroy(b->plan_z2d);
+  }
+  if (b->d_real) g_cu.cuda_free(b->d_real);
+  if (b->d_cplx) g_cu.cuda_free(b->d_cplx);
+}
+
+/* CufftBackend::r2c_3d / c2r_3d (cufft.rs:249-319).  Failures abort the
+ * transform with a message (the reference panics). */
+static void cufft_r2c(const backend* b, const double* in, cpx* out) {
+  const size_t nreal = (size_t)b->nx * b->ny * b->nz, ncplx = (size_t)b->nx * b->ny * b->hz;
+  int rc = g_cu.cuda_memcpy(b->d_real, in, nreal * sizeof(double), MEMCPY_H2D_);
+  if (rc == 0) rc = g_cu.exec_d2z(b->plan_d2z, (double*)b->d_real, b->d_cplx);
+  if (rc == 0) rc = g_cu.cuda_memcpy(out, b->d_cplx, ncplx * sizeof(cpx), MEMCPY_D2H_);
+  if (rc != 0) { fprintf(stderr, "cuFFT r2c failed: %d\n", rc); abort(); }
+}
+
+static void cufft_c2r(const backend* b, const cpx* in, double* out) {
+  const size_t nreal = (size_t)b->nx * b->ny * b->nz, ncplx = (size_t)b->nx * b->ny * b->hz;
+  int rc = g_cu.cuda_memcpy(b->d_cplx, in, ncplx * sizeof(cpx), MEMCPY_H2D_);
+  if (rc == 0) rc = g_cu.exec_z2d(b->plan_z2d, b->d_cplx, (double*)b->d_real);
+  if (rc == 0) rc = g_cu.cuda_memcpy(out, b->d_real, nreal * sizeof(double), MEMCPY_D2H_);
+  if (rc != 0) { fprintf(stderr, "cuFFT c2r failed: %d\n", rc); abort(); }
+  const double n_total = (double)nreal;
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)nreal; ++i) out[i] = out[i] / n_total;
+}
 
 static int maxi(int a, int b) { return a > b ? a : b; }
 
@@ -225,6 +342,7 @@ static void c2c_axis(const backend* b, int axis, const cpx* src, cpx* dst, int i
 }
 
 static void r2c_3d(const backend* b, const double* in, cpx* out) {
+  if (b->cufft) { cufft_r2c(b, in, out); return; }
   const size_t nc = (size_t)b->nx * b->ny * b->hz;
   cpx* temp_rz = (cpx*)calloc(nc, sizeof(cpx));
 #pragma omp parallel
@@ -244,6 +362,7 @@ static void r2c_3d(const backend* b, const double* in, cpx* out) {
 }
 
 static void c2r_3d(const backend* b, const cpx* in, double* out) {
+  if (b->cufft) { cufft_c2r(b, in, out); return; }
   const size_t nc = (size_t)b->nx * b->ny * b->hz;
   cpx* temp_ix = (cpx*)calloc(nc, sizeof(cpx));
   c2c_axis(b, 0, in, temp_ix, 1);
@@ -603,6 +722,66 @@ int vkc_nonlinear(void* h, const double* ux, const double* uy, const double* uz,
   cpx* in[3] = {(cpx*)ux, (cpx*)uy, (cpx*)uz};
   cpx* out[3] = {(cpx*)ox, (cpx*)oy, (cpx*)oz};
   compute_nonlinear(s, in, out);
+  return 0;
+}
+
+/* Backend mode of the solvers created afterwards: 0 = the CPU FFT (the
+ * reference's ndrustfft backend), 1 = the reference's cuFFT backend pattern.
+ * Returns 0, or 1 with a message in vkc_cufft_error() when the CUDA
+ * libraries cannot be loaded. */
+int vkc_set_cufft(int on) {
+  if (on && cu_load() != 0) return 1;
+  g_use_cufft = on ? 1 : 0;
+  return 0;
+}
+
+const char* vkc_cufft_error(void) { return g_cu_err; }
+
+/* 1 if the solver's transforms run through cuFFT. */
+int vkc_uses_cufft(void* h) { return ((solver*)h)->fft_padded.cufft && ((solver*)h)->fft.cufft; }
+
+/* energy_spectrum (vonkarman-diag/src/spectrum.rs:13-60): shell round(|k|),
+ * E_s += 0.5 w |u|^2 / N^6.  Per-thread histograms over x planes, added in
+ * thread order. */
+int vkc_spectrum(void* h, double* out, int nsh) {
+  solver* s = (solver*)h;
+  const int n = s->n, hz = s->h;
+  const double ntot = (double)n * (double)n * (double)n;
+  const double kmx = (double)(n / 2);
+  const int want = (int)ceil(sqrt(kmx * kmx + kmx * kmx + kmx * kmx)) + 1;
+  if (nsh < want) return 1;
+  int nt = 1;
+#ifdef _OPENMP
+  nt = omp_get_max_threads();
+#endif
+  double* hist = (double*)calloc((size_t)nt * want, sizeof(double));
+#pragma omp parallel
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    double* my = hist + (size_t)t * want;
+#pragma omp for schedule(static)
+    for (int ix = 0; ix < n; ++ix)
+      for (int iy = 0; iy < n; ++iy)
+        for (int iz = 0; iz < hz; ++iz) {
+          const double kx = s->kx[ix], ky = s->ky[iy], kz = s->kz[iz];
+          const int shell = (int)round(sqrt(kx * kx + ky * ky + kz * kz));
+          if (shell >= want) continue;
+          const size_t i = ((size_t)ix * n + iy) * hz + iz;
+          double mag2 = 0.0;
+          for (int c = 0; c < 3; ++c) mag2 += s->u[c][i].re * s->u[c][i].re + s->u[c][i].im * s->u[c][i].im;
+          const double w = (iz == 0 || iz == n / 2) ? 1.0 : 2.0;
+          my[shell] += 0.5 * w * mag2 / (ntot * ntot);
+        }
+  }
+  for (int k = 0; k < want; ++k) {
+    double acc = 0.0;
+    for (int t = 0; t < nt; ++t) acc += hist[(size_t)t * want + k];
+    out[k] = acc;
+  }
+  free(hist);
   return 0;
 }
 

@@ -41,6 +41,10 @@ def load():
         lib.vkc_max_threads.restype = ctypes.c_int
         lib.vkc_r2c_3d.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _DP, _DP]
         lib.vkc_c2r_3d.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _DP, _DP]
+        lib.vkc_set_cufft.argtypes = [ctypes.c_int]
+        lib.vkc_cufft_error.restype = ctypes.c_char_p
+        lib.vkc_uses_cufft.argtypes = [ctypes.c_void_p]
+        lib.vkc_spectrum.argtypes = [ctypes.c_void_p, _DP, ctypes.c_int]
         _lib = lib
     return _lib
 
@@ -55,6 +59,16 @@ def set_threads(t: int):
 
 def max_threads() -> int:
     return int(load().vkc_max_threads())
+
+
+def set_cufft(on: bool):
+    """Route the 3-D transforms of solvers created afterwards through the
+    reference's cuFFT backend pattern (vonkarman-fft/src/cufft.rs: per-call
+    host <-> device copies around cufftExecD2Z / Z2D, host normalisation).
+    Raises RuntimeError when libcudart / libcufft cannot be loaded."""
+    lib = load()
+    if lib.vkc_set_cufft(1 if on else 0) != 0:
+        raise RuntimeError(lib.vkc_cufft_error().decode(errors="replace"))
 
 
 class CpuSolver:
@@ -84,6 +98,17 @@ class CpuSolver:
         out = [np.empty(shp, np.complex128) for _ in range(3)]
         self.lib.vkc_nonlinear(self.h, *[_p(c) for c in ins], *[_p(c) for c in out])
         return out
+
+    def spectrum(self):
+        """energy_spectrum of the current state (spectrum.rs:13-60)."""
+        kmx = float(self.n // 2)
+        nsh = int(math.ceil(math.sqrt(3.0 * kmx * kmx))) + 1
+        out = np.empty(nsh)
+        self.lib.vkc_spectrum(self.h, _p(out), nsh)
+        return out
+
+    def uses_cufft(self) -> bool:
+        return bool(self.lib.vkc_uses_cufft(self.h))
 
     def time(self):
         return self.lib.vkc_time(self.h)

@@ -464,6 +464,19 @@ class Periodic3D:
                     cfl_number=mw * self.dt / self.grid.dx)
 
 
+def tier1_of_state(grid: Grid, nu: float, u_hat, time: float, step_count: int, dt: float) -> dict:
+    """``ScalarDiagnostics::from_domain`` (vonkarman-diag/src/scalar.rs:22-54) of a
+    given state with its time, step count and dt, without building the
+    per-mode ETD table of ``Periodic3D.__init__`` (large grids)."""
+    p = Periodic3D.__new__(Periodic3D)
+    p.grid = grid
+    p.nu = float(nu)
+    p.ops = SpectralOps(grid)
+    p.u_hat = [np.asarray(c, dtype=np.complex128) for c in u_hat]
+    p.time, p.step_count, p.dt = float(time), int(step_count), float(dt)
+    return p.tier1()
+
+
 def rk4_step(u_hat, ops: SpectralOps, nu: float, dt: float):
     """Classical RK4 on L + N (rk4.rs:16-146)."""
     k2 = ops.k_mag_sq

@@ -1,6 +1,8 @@
 """GPU parity: the CUDA path (through the C ABI) against the numpy oracle on
-the same inputs.  Norm-relative errors: ||a - b||_2 / ||b||_2 over all
-components (element-wise relative error is ill-posed for the ~0 modes).
+the same inputs.  FP64 comparisons bound two errors: norm-relative
+||a - b||_2 / ||b||_2 over all components, and per coefficient
+max |a - b| / max |b| (element-wise relative error is ill-posed for the ~0
+modes; the max-coefficient form still sees a large error on a few modes).
 
 Tolerances (FP64): 1e-12 for spectral coefficients after one step or one
 nonlinear evaluation, 1e-10 for Tier-1 diagnostics and E(k); FP32-bulk: 2e-5
@@ -25,6 +27,20 @@ def nrel(a, b):
     num = math.sqrt(sum(float(np.sum(np.abs(x - y) ** 2)) for x, y in zip(a, b)))
     den = math.sqrt(sum(float(np.sum(np.abs(y) ** 2)) for y in b))
     return num / den if den > 0 else num
+
+
+def maxcoef(a, b):
+    """max |a - b| / max |b| over all coefficients of all components: a large
+    error on a few small coefficients cannot hide behind the norm."""
+    num = max(float(np.max(np.abs(x - y))) for x, y in zip(a, b))
+    den = max(float(np.max(np.abs(y))) for y in b)
+    return num / den if den > 0 else num
+
+
+def close(a, b, tol):
+    """Both metrics within tol."""
+    e1, e2 = nrel(a, b), maxcoef(a, b)
+    assert e1 < tol and e2 < tol, (e1, e2, tol)
 
 
 def rel(a, b):
@@ -56,7 +72,7 @@ def test_fft_r2c_c2r_vs_numpy(vk, shape):
     f = vk.GpuFftBackend(*shape)
     xh = f.r2c_3d(x)
     ref = np.fft.rfftn(x)
-    assert nrel([xh], [ref]) < TOL64
+    close([xh], [ref], TOL64)
     back = f.c2r_3d(xh)
     assert np.abs(back - x).max() < 1e-12 * max(1.0, np.abs(x).max())
     # c2r of a non-Hermitian input: imaginary parts of DC/Nyquist planes ignored
@@ -78,7 +94,10 @@ def test_fft_all_line_lengths_vs_numpy(vk, precision, tol, shape):
     x = rng.standard_normal(shape)
     f = vk.GpuFftBackend(*shape, precision=precision)
     ref = np.fft.rfftn(x)
-    assert nrel([f.r2c_3d(x)], [ref]) < tol
+    xh = f.r2c_3d(x)
+    assert nrel([xh], [ref]) < tol
+    if precision == "fp64":
+        assert maxcoef([xh], [ref]) < tol
     assert np.abs(f.c2r_3d(ref) - x).max() < 100 * tol * max(1.0, np.abs(x).max())
     f.close()
 
@@ -118,7 +137,7 @@ def test_nonlinear_vs_oracle(vk, n):
     want = vo.compute_nonlinear(vo.SpectralOps(g), u)
     s = vk.Periodic3D(vk.GridSpec(n), 0.01, u, vk.SolverOptions(dt_mode="fixed", dt_fixed=1e-3))
     got = vk.compute_nonlinear(s, u)
-    assert nrel(got, want) < TOL64
+    close(got, want, TOL64)
     s.close()
 
 
@@ -130,7 +149,10 @@ def test_nonlinear_vs_oracle_n128(vk, precision, tol):
     want = vo.compute_nonlinear(vo.SpectralOps(g), u)
     s = vk.Periodic3D(vk.GridSpec(n), 0.01, u, vk.SolverOptions(precision=precision, dt_mode="fixed",
                                                                    dt_fixed=1e-3))
-    assert nrel(vk.compute_nonlinear(s, u), want) < tol
+    got = vk.compute_nonlinear(s, u)
+    assert nrel(got, want) < tol
+    if precision == "fp64":
+        assert maxcoef(got, want) < tol
     s.close()
 
 
@@ -158,7 +180,7 @@ def test_nonlinear_non_hermitian_input(vk):
     u = random_state(n, 7, clean=False)
     want = vo.compute_nonlinear(vo.SpectralOps(g), u)
     s = vk.Periodic3D(vk.GridSpec(n), 0.01, u, vk.SolverOptions(dt_mode="fixed", dt_fixed=1e-3))
-    assert nrel(vk.compute_nonlinear(s, u), want) < TOL64
+    close(vk.compute_nonlinear(s, u), want, TOL64)
 
 
 def test_nonlinear_divergence_free_kat(vk):
@@ -188,7 +210,7 @@ def test_dealiased_zero_and_antisymmetry_kats(vk):
     u[1][n - 2, 1, 3] = -2.0 + 0.5j
     u[2][3, n - 1, 4] = 1.5 - 0.7j  # z-Nyquist plane (iz = n/2)
     want = vo.compute_nonlinear(vo.SpectralOps(g), u)
-    assert nrel(vk.compute_nonlinear(s, u), want) < TOL64
+    close(vk.compute_nonlinear(s, u), want, TOL64)
 
 
 # --- one step / many steps ---------------------------------------------------
@@ -202,7 +224,7 @@ def test_one_step_taylor_green_n64_fixed_dt(vk):
     ref.step()
     s = vk.Periodic3D(vk.GridSpec(n), nu, u0, vk.SolverOptions(dt_mode="fixed", dt_fixed=dt))
     s.step()
-    assert nrel(s.u_hat(), ref.u_hat) < TOL64
+    close(s.u_hat(), ref.u_hat, TOL64)
     assert s.time() == pytest.approx(dt, rel=0, abs=0)
 
 
@@ -244,7 +266,7 @@ def test_steps_random_cfl_vs_oracle(vk, n):
     for _ in range(5):
         ref.step()
     s.step(5)
-    assert nrel(s.u_hat(), ref.u_hat) < 1e-11
+    close(s.u_hat(), ref.u_hat, 1e-11)
     assert rel(s.dt(), ref.dt) < 1e-12
     assert rel(s.time(), ref.time) < 1e-12
     assert s.step_count() == 5
@@ -261,7 +283,7 @@ def test_etd_variants_vs_oracle(vk, variant):
     for _ in range(3):
         ref.step()
     s.step(3)
-    assert nrel(s.u_hat(), ref.u_hat) < TOL64
+    close(s.u_hat(), ref.u_hat, TOL64)
 
 
 def test_rk4_vs_oracle(vk):
@@ -274,7 +296,7 @@ def test_rk4_vs_oracle(vk):
     for _ in range(3):
         ref.step()
     s.step(3)
-    assert nrel(s.u_hat(), ref.u_hat) < TOL64
+    close(s.u_hat(), ref.u_hat, TOL64)
 
 
 def test_tier1_and_spectrum_vs_oracle(vk):

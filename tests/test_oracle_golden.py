@@ -93,3 +93,19 @@ def test_c_port_nonlinear_and_steps_match_oracle(cpu, n):
         o.step()
     assert nrel(s.u_hat(), o.u_hat) < 1e-13
     assert abs(s.time() - o.time) <= 1e-14 * o.time
+
+
+def test_c_restatement_spectrum_vs_numpy_oracle():
+    """vkc_spectrum (energy_spectrum, spectrum.rs:13-60, in the C restatement
+    the reference arm of bench.py times) against the numpy oracle."""
+    from oracle import vk_cpu
+
+    n = 32
+    g = vo.Grid(n, 3.0)
+    u = vo.hermitian_clean(g, vo.random_field(g, 8, amp=100.0))
+    c = vk_cpu.CpuSolver(n, 0.01, u, l=3.0)
+    got = c.spectrum()
+    c.close()
+    _, want = vo.energy_spectrum(u, vo.SpectralOps(g))
+    assert got.shape == want.shape
+    assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()

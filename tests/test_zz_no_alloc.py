@@ -20,26 +20,34 @@ pytestmark = pytest.mark.gpu
 TOL_DIAG = 1e-10
 
 
-def test_spectrum_noalloc_matches_vk_spectrum():
+@pytest.mark.parametrize("precision", ["fp64", "fp32bulk"])
+def test_spectrum_noalloc_matches_vk_spectrum(precision):
+    """Both precisions: the FP32-bulk state is handed over as the complex64
+    values the solver holds (an exact round trip through the FP64 host copy),
+    so both entry points form the same FP32 per-mode products and differ only
+    in the order of their FP64 sums."""
     torch = pytest.importorskip("torch")
     import vonkarman_gb300 as vk
     from vonkarman_gb300 import _native as nat
 
     lib = nat.load()
+    code = nat.PRECISION[precision]
     for n, seed in ((32, 21), (64, 22)):
         g = vo.Grid(n)
         u0 = vo.hermitian_clean(g, vo.random_field(g, seed, amp=float(n) ** 3 / 50.0))
-        s = vk.Periodic3D(vk.GridSpec(n), 0.01, u0)
+        s = vk.Periodic3D(vk.GridSpec(n), 0.01, u0, vk.SolverOptions(precision=precision))
         s.step(2)
         _, want = vk.energy_spectrum(s)
         state = np.ascontiguousarray(np.stack(s.u_hat()))
         s.close()
+        if precision == "fp32bulk":
+            state = state.astype(np.complex64)
         dev_u = torch.from_numpy(state).to("cuda")
         out = torch.empty(len(want), dtype=torch.float64, device="cuda")
         for _ in range(2):
             out.fill_(float("nan"))
             torch.cuda.synchronize()
-            rc = lib.vk_spectrum_noalloc(ctypes.c_void_p(dev_u.data_ptr()), n, 2.0 * math.pi, 0,
+            rc = lib.vk_spectrum_noalloc(ctypes.c_void_p(dev_u.data_ptr()), n, 2.0 * math.pi, code,
                                          ctypes.c_void_p(out.data_ptr()), None)
             assert rc == 0, lib.vk_last_error(None)
             torch.cuda.synchronize()

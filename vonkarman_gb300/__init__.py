@@ -13,6 +13,8 @@ from .solver import (  # noqa: F401
     Periodic3D,
     ScalarDiagnostics,
     SolverOptions,
+    SpectralOps,
+    apply_viscous,
     compensated_spectrum,
     compute_nonlinear,
     create_backend,
@@ -20,9 +22,11 @@ from .solver import (  # noqa: F401
     energy_spectrum,
     l2_inner,
     nonlinear_adjoint,
+    spectral_ops,
 )
 from . import ics  # noqa: F401
 
-__all__ = ["GridSpec", "GpuFftBackend", "Periodic3D", "ScalarDiagnostics", "SolverOptions",
+__all__ = ["GridSpec", "GpuFftBackend", "Periodic3D", "ScalarDiagnostics", "SolverOptions", "SpectralOps",
+           "apply_viscous", "spectral_ops",
            "compensated_spectrum", "compute_nonlinear", "create_backend", "dissipation_spectrum",
            "energy_spectrum", "ics", "l2_inner", "nonlinear_adjoint"]

@@ -70,6 +70,8 @@ SIGNATURES = {
     "vk_spectrum_len": (c_int, [_CTX, POINTER(c_int32)]),
     "vk_spectrum": (c_int, [_CTX, _DP, _DP, c_int32]),
     "vk_nonlinear_host": (c_int, [_CTX, _DP, _DP, _DP, _DP, _DP, _DP]),
+    "vk_apply_viscous_host": (c_int, [_CTX, c_double, _DP, _DP, _DP, _DP, _DP, _DP]),
+    "vk_wavenumbers": (c_int, [_CTX, _DP, _DP, _DP, _DP]),
     "vk_adjoint_forward": (c_int, [_CTX, c_int64, c_int32, _DP]),
     "vk_adjoint_set_schedule": (c_int, [_CTX, c_int32]),
     "vk_adjoint_backward": (c_int, [_CTX, _DP, _DP, _DP]),

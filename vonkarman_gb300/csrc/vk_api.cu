@@ -238,6 +238,7 @@ vk::StageArgs<R> stage_args(vk_ctx* c, int op, void* out) {
   s.etd = c->etd;
   s.dt = &c->dsc->dt;
   s.nu = c->cfg.nu;
+  s.nonfinite = &c->dsc->nonfinite;
   return s;
 }
 
@@ -369,9 +370,16 @@ void fill_tier1(const vk_ctx* c, const vk::DevScalars& d, uint64_t step, vk_tier
   o->cfl_number = o->max_vorticity * o->dt / dx_of(c);
 }
 
+// Device scalars of the context after a synchronisation.  A NaN or infinity
+// seen in the state since it was set (by a CFL / max pass or by the final
+// stage of a step) is reported here, at the first synchronising call after
+// it: the checks of the reference's audit (vonkarman-diag/src/audit.rs:175-197)
+// without a per-step readback.
 int read_scalars(vk_ctx* c, vk::DevScalars* h) {
   VK_CHECK(c, cudaMemcpyAsync(h, c->dsc, sizeof(vk::DevScalars), cudaMemcpyDeviceToHost, c->stream));
   VK_CHECK(c, cudaStreamSynchronize(c->stream));
+  if (h->nonfinite || h->mx.nan_flag)
+    return fail(c, VK_ERR_NONFINITE, "non-finite value (NaN or Inf) in the solver state");
   return VK_OK;
 }
 
@@ -698,17 +706,15 @@ int vk_run(vk_ctx* c, int64_t nsteps, int64_t every, vk_tier1_out* out, int64_t 
       ++nrec;
     }
   }
-  if (nrec > 0) {
-    std::vector<vk::DevScalars> h((size_t)nrec);
+  std::vector<vk::DevScalars> h((size_t)nrec);
+  if (nrec > 0)
     VK_CHECK(c, cudaMemcpyAsync(h.data(), c->records, (size_t)nrec * sizeof(vk::DevScalars), cudaMemcpyDeviceToHost,
                                 c->stream));
-    VK_CHECK(c, cudaStreamSynchronize(c->stream));
-    for (int64_t r = 0; r < nrec; ++r) fill_tier1(c, h[r], steps[r], out + r);
-  } else {
-    VK_CHECK(c, cudaStreamSynchronize(c->stream));
-  }
+  vk::DevScalars last;
+  const int r = read_scalars(c, &last);   // synchronises; NaN / Inf -> VK_ERR_NONFINITE
+  for (int64_t k = 0; k < nrec; ++k) fill_tier1(c, h[(size_t)k], steps[(size_t)k], out + k);
   if (n_records) *n_records = nrec;
-  return VK_OK;
+  return r;
 }
 
 int vk_spectrum_len(const vk_ctx* c, int32_t* n) {
@@ -751,6 +757,38 @@ int vk_nonlinear_host(vk_ctx* c, const double* ux, const double* uy, const doubl
   if (r != VK_OK) return r;
   VK_CHECK(c, nle(c, c->temp, vk::ST_NL_OUT, c->n1));
   return download_state(c, c->n1, ox, oy, oz);
+}
+
+int vk_apply_viscous_host(vk_ctx* c, double nu, const double* ux, const double* uy, const double* uz, double* ox,
+                          double* oy, double* oz) {
+  if (!c) return VK_ERR_INVALID;
+  if (!std::isfinite(nu)) return fail(c, VK_ERR_INVALID, "nu must be finite");
+  DeviceGuard g(c->cfg.device);
+  // temp holds the input, n1 receives the output: the solver state u is untouched.
+  int r = upload_state(c, c->temp, ux, uy, uz);
+  if (r != VK_OK) return r;
+  VK_CHECK(c, vk::launch_apply_viscous(c->n1, c->temp, c->fp32 ? 1 : 0, c->N, c->cs, c->ks, nu, c->stream));
+  return download_state(c, c->n1, ox, oy, oz);
+}
+
+int vk_wavenumbers(vk_ctx* c, double* kx, double* ky, double* kz, double* k_mag_sq) {
+  if (!c || !kx || !ky || !kz) return VK_ERR_INVALID;
+  // rfftfreq_full / rfftfreq_half (spectral_ops.rs:51-74): index * (2 pi / L),
+  // index n/2 .. n-1 of the full axes mapped to -n/2 .. -1
+  const int n = c->N;
+  for (int i = 0; i < n; ++i) {
+    const double k = (double)(i < n / 2 ? i : i - n) * c->ks;
+    kx[i] = k;
+    ky[i] = k;
+  }
+  for (int i = 0; i < c->H; ++i) kz[i] = (double)i * c->ks;
+  if (!k_mag_sq) return VK_OK;
+  DeviceGuard g(c->cfg.device);
+  // |k|^2 per mode on the device (bufA holds cs doubles at least), read back
+  VK_CHECK(c, vk::launch_k_mag_sq((double*)c->bufA, n, c->ks, c->stream));
+  VK_CHECK(c, cudaMemcpyAsync(k_mag_sq, c->bufA, c->cs * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  VK_CHECK(c, cudaStreamSynchronize(c->stream));
+  return VK_OK;
 }
 
 }  // extern "C"
@@ -1031,7 +1069,8 @@ int vk_step_timed(vk_ctx* c, int64_t nsteps, double* elapsed_ms) {
   float ms = 0.f;
   VK_CHECK(c, cudaEventElapsedTime(&ms, c->tev[0], c->tev[1]));
   *elapsed_ms = ms;
-  return VK_OK;
+  vk::DevScalars h;
+  return read_scalars(c, &h);
 }
 
 int vk_profile_enable(vk_ctx* c, int32_t enable) {

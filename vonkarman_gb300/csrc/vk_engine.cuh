@@ -4,6 +4,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include "vk_adjoint.cuh"
@@ -16,17 +17,19 @@ namespace vk {
 // below 64, one cache per kernel instance).  Kernels with static shared
 // memory as well need the opt-in below 48 KB of dynamic memory too, so any
 // sizeable request opts in.
+// The mask is atomic: contexts on several host threads (and the
+// allocation-free entry point, from any thread) share these instances.
 template <auto KERN>
 inline cudaError_t prepare_kernel(size_t smem) {
-  static unsigned long long done_mask = 0ull;
+  static std::atomic<unsigned long long> done_mask{0ull};
   if (smem <= 16 * 1024) return cudaSuccess;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   const unsigned long long bit = dev < 64 ? (1ull << dev) : 0ull;
-  if (bit && (done_mask & bit)) return cudaSuccess;
+  if (bit && (done_mask.load(std::memory_order_acquire) & bit)) return cudaSuccess;
   e = cudaFuncSetAttribute(KERN, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e == cudaSuccess) done_mask |= bit;
+  if (e == cudaSuccess) done_mask.fetch_or(bit, std::memory_order_acq_rel);
   return e;
 }
 

@@ -28,7 +28,7 @@ struct DevScalars {
   double time;            // accumulated time
   double cfl_dt;          // last CFL estimate
   int etd_recompute;      // set by the CFL update, read by the ETD table kernel
-  int pad0;
+  int nonfinite;          // sticky: a NaN/Inf was seen in the state (CFL maxima or a step's output)
   MaxOut mx;              // N-grid maxima of the current state
   double sums[4];         // Tier-1 sums (energy, enstrophy, helicity, superhelicity), raw
 };
@@ -62,6 +62,7 @@ template <typename R> struct StageArgs {
   const double* etd;               // table, ETD_STRIDE doubles per |k|^2 index
   const double* dt;                // device scalar
   double nu;
+  int* nonfinite;                  // set when a final stage writes a non-finite value (null: no check)
 };
 
 // Per-pass timing hook (profiling mode): brackets each kernel launch with
@@ -163,7 +164,13 @@ cudaError_t launch_etd_table(double* tab, int nent, double nu, double ks2, const
 cudaError_t launch_cfl_update(DevScalars* d, double dx, double nu, double safety, int mode, cudaStream_t s);
 cudaError_t launch_reset_max(DevScalars* d, cudaStream_t s);
 cudaError_t launch_time_advance(DevScalars* d, cudaStream_t s);
-cudaError_t launch_reduce_columns(const double* part, int nblk, int width, double* out, cudaStream_t s);
+cudaError_t launch_reduce_columns(const double* part, int nblk, int width, double* out, cudaStream_t s,
+                                  double scale = 1.0);
+// |k|^2 of every mode of an (n, n, n/2+1) grid (SpectralOps::k_mag_sq) and
+// SpectralOps::apply_viscous on a device vector field (fp32: float2 data).
+cudaError_t launch_k_mag_sq(double* out, int n, double ks, cudaStream_t s);
+cudaError_t launch_apply_viscous(void* out, const void* in, int fp32, int n, size_t cs, double ks, double nu,
+                                 cudaStream_t s);
 // complex arrays: fp32 flags select float2 (1) or double2 (0)
 cudaError_t launch_convert_c(void* out, int out_fp32, const void* in, int in_fp32, size_t n, cudaStream_t s);
 cudaError_t launch_convert_r(void* out, int out_fp32, const void* in, int in_fp32, size_t n, cudaStream_t s);

@@ -218,6 +218,15 @@ __device__ __forceinline__ C2<R> axpby(R a, C2<R> x, R b, C2<R> y) {
   return cmk<R>(a * x.x + b * y.x, a * x.y + b * y.y);
 }
 
+// The final stage of a step raises the context's sticky non-finite flag when
+// it writes a NaN or an infinity (the NaN check of the reference's audit,
+// vonkarman-diag/src/audit.rs:175-197, without a readback); the atomic runs
+// only on that rare path.
+template <typename R>
+__device__ __forceinline__ void flag_nonfinite(const StageArgs<R>& s, C2<R> v) {
+  if (!(isfinite(v.x) && isfinite(v.y)) && s.nonfinite) atomicOr(s.nonfinite, 1);
+}
+
 // Stage epilogue of NM modes at once: the inputs of all modes and all three
 // components are loaded before any result is stored (a store may alias a
 // later load as far as the compiler knows, so interleaving them would
@@ -272,7 +281,9 @@ __device__ __forceinline__ void stage_apply_n(const StageArgs<R>& s, const size_
           s.temp[i] = cmk<R>(u[q][c].x + h * rhs.x, u[q][c].y + h * rhs.y);
         } else {
           const R sixth = (R)(dt / 6.0);
-          s.u[i] = cmk<R>(u[q][c].x + sixth * (a[q][c].x + rhs.x), u[q][c].y + sixth * (a[q][c].y + rhs.y));
+          const C2<R> un = cmk<R>(u[q][c].x + sixth * (a[q][c].x + rhs.x), u[q][c].y + sixth * (a[q][c].y + rhs.y));
+          s.u[i] = un;
+          flag_nonfinite<R>(s, un);
         }
       }
     }
@@ -361,7 +372,9 @@ __device__ __forceinline__ void stage_apply_n(const StageArgs<R>& s, const size_
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const C2<R> rhs = cmk<R>(a[q][c].x + b4[q] * nl[q][c].x, a[q][c].y + b4[q] * nl[q][c].y);
-          s.u_out[c * cs + idx[q]] = axpby<R>(ef[q], u[q][c], (R)dt, rhs);
+          const C2<R> un = axpby<R>(ef[q], u[q][c], (R)dt, rhs);
+          s.u_out[c * cs + idx[q]] = un;
+          flag_nonfinite<R>(s, un);
         }
       }
       break;

@@ -75,6 +75,9 @@ __global__ void k_etd_table(double* __restrict__ tab, int nent, double nu, doubl
 // 1 = initialise (Periodic3D::new, solver.rs:88-93), 2 = estimate only.
 __global__ void k_cfl_update(DevScalars* d, double dx, double nu, double safety, int mode) {
   const double umax = sqrt(__longlong_as_double((long long)d->mx.umax2));
+  // a NaN never wins the maxima (fmax drops it; the pass raises nan_flag) and
+  // an infinity does: either marks the state non-finite for the host
+  if (d->mx.nan_flag || !isfinite(umax)) d->nonfinite = 1;
   const double adv = umax > 1e-30 ? dx / umax : 1.0;
   const double visc = nu > 1e-30 ? dx * dx / nu : INFINITY;
   const double nd = safety * fmin(fmin(adv, visc), 0.1);
@@ -96,9 +99,11 @@ __global__ void k_reset_max(DevScalars* d) {
 
 __global__ void k_time_advance(DevScalars* d) { d->time += d->dt; }
 
-// Reduce part[nblk][width] column-wise in a fixed order into out[width].
+// Reduce part[nblk][width] column-wise in a fixed order into
+// out[width] = scale * sum (Neumaier-compensated per thread, then a fixed
+// pairwise tree).
 __global__ void __launch_bounds__(RED_THREADS)
-k_reduce_columns(const double* __restrict__ part, int nblk, int width, double* __restrict__ out) {
+k_reduce_columns(const double* __restrict__ part, int nblk, int width, double scale, double* __restrict__ out) {
   __shared__ double sm[RED_THREADS];
   for (int col = blockIdx.x; col < width; col += gridDim.x) {
     Neu a = {0, 0};
@@ -109,8 +114,48 @@ k_reduce_columns(const double* __restrict__ part, int nblk, int width, double* _
       if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
       __syncthreads();
     }
-    if (threadIdx.x == 0) out[col] = sm[0];
+    if (threadIdx.x == 0) out[col] = scale * sm[0];
     __syncthreads();
+  }
+}
+
+// |k|^2 of mode (ix, iy, iz) as SpectralOps::new forms it
+// (vonkarman-core/src/spectral_ops.rs:26-44, 51-74): k = index * (2 pi / L)
+// with index n/2 mapped to -n/2, kx^2 + ky^2 + kz^2 summed left to right,
+// every operation rounded once (no contraction), so the FP64 values are the
+// reference's bit for bit.
+__device__ __forceinline__ double k_mag_sq_of(int ix, int iy, int iz, int n, double ks) {
+  const double kx = __dmul_rn((double)signed_k(ix, n), ks);
+  const double ky = __dmul_rn((double)signed_k(iy, n), ks);
+  const double kz = __dmul_rn((double)iz, ks);
+  return __dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz));
+}
+
+__global__ void k_k_mag_sq(double* __restrict__ out, int n, double ks) {
+  const int h = n / 2 + 1;
+  const size_t total = (size_t)n * n * h;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int iz = (int)(i % h);
+    const size_t row = i / h;
+    out[i] = k_mag_sq_of((int)(row / n), (int)(row % n), iz, n, ks);
+  }
+}
+
+// SpectralOps::apply_viscous (spectral_ops.rs:154-175): out_c = -(nu |k|^2) u_c
+// for the three components (component stride cs).
+template <typename R>
+__global__ void k_apply_viscous(C2<R>* __restrict__ out, const C2<R>* __restrict__ in, int n, size_t cs, double ks,
+                                double nu) {
+  const int h = n / 2 + 1;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cs; i += (size_t)gridDim.x * blockDim.x) {
+    const int iz = (int)(i % h);
+    const size_t row = i / h;
+    const R f = (R)(-__dmul_rn(nu, k_mag_sq_of((int)(row / n), (int)(row % n), iz, n, ks)));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const C2<R> v = in[c * cs + i];
+      out[c * cs + i] = cmk<R>(f * v.x, f * v.y);
+    }
   }
 }
 
@@ -152,15 +197,30 @@ cudaError_t launch_time_advance(DevScalars* d, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_reduce_columns(const double* part, int nblk, int width, double* out, cudaStream_t s) {
+cudaError_t launch_reduce_columns(const double* part, int nblk, int width, double* out, cudaStream_t s,
+                                  double scale) {
   const int nb = width < 1024 ? width : 1024;
-  k_reduce_columns<<<nb, RED_THREADS, 0, s>>>(part, nblk, width, out);
+  k_reduce_columns<<<nb, RED_THREADS, 0, s>>>(part, nblk, width, scale, out);
   return cudaGetLastError();
 }
 
 static int conv_blocks(size_t n) {
   const size_t nb = (n + 255) / 256;
   return (int)(nb < 65536 ? nb : 65536);
+}
+
+cudaError_t launch_k_mag_sq(double* out, int n, double ks, cudaStream_t s) {
+  k_k_mag_sq<<<conv_blocks((size_t)n * n * (n / 2 + 1)), 256, 0, s>>>(out, n, ks);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apply_viscous(void* out, const void* in, int fp32, int n, size_t cs, double ks, double nu,
+                                 cudaStream_t s) {
+  if (fp32)
+    k_apply_viscous<float><<<conv_blocks(cs), 256, 0, s>>>((float2*)out, (const float2*)in, n, cs, ks, nu);
+  else
+    k_apply_viscous<double><<<conv_blocks(cs), 256, 0, s>>>((double2*)out, (const double2*)in, n, cs, ks, nu);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_convert_c(void* out, int out_fp32, const void* in, int in_fp32, size_t n, cudaStream_t s) {

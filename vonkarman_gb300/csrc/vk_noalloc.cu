@@ -26,26 +26,56 @@ constexpr int kNoallocMaxShells = 448;  // ceil(sqrt(3) * 512 / 2) + 1 = 445 fit
 
 static __device__ __align__(256) double g_spectrum_scratch[kNoallocBlocks * kNoallocMaxShells];
 
+// Device address of the scratch per device ordinal, valid for the CUDA
+// context it was looked up in: a context torn down and created again (a
+// device reset) loads the module again, possibly elsewhere, so the address is
+// looked up again whenever the current context's unique id has changed.
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;
+  double* ptr = nullptr;
+};
 std::mutex g_scratch_mu;
-double* g_scratch_addr[64] = {};  // device address of the scratch, per device ordinal
+ScratchAddr g_scratch_addr[64];
 
-// One CTA per shell: fixed-order sum of the nblk partials of that shell, then
-// the 1/2 and 1/N^6 of spectrum.rs:53.  Every partial is rewritten by each
-// call, so the shared scratch needs no clearing between calls.
-__global__ void __launch_bounds__(256)
-k_noalloc_spectrum_finish(const double* __restrict__ part, int nblk, int nsh, double scale,
-                          double* __restrict__ out) {
-  __shared__ double sm[256];
-  const int col = blockIdx.x;
-  double s = 0.0;
-  for (int b = threadIdx.x; b < nblk; b += 256) s += part[(size_t)b * nsh + col];
-  sm[threadIdx.x] = s;
-  __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
-    __syncthreads();
+using CtxGetIdFn = int (*)(void* ctx, unsigned long long* id);   // cuCtxGetId
+
+// Unique id of the current context (cuCtxGetId, reached through the runtime's
+// driver entry point so that the library links only the CUDA runtime); 0 when
+// no context is current yet or the driver lacks the call.
+unsigned long long current_ctx_id() {
+  static const CtxGetIdFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetIdFn>(p);
+  }();
+  unsigned long long id = 0;
+  if (!fn || fn(nullptr, &id) != 0) return 0;
+  return id;
+}
+
+// Set-up of the current device: the scratch's device address in the current
+// context.  cudaGetSymbolAddress also loads the module into the context when
+// it is not loaded yet, which is why the first call on a device should come
+// before any stream capture.
+cudaError_t scratch_address(int dev, double** out) {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  ScratchAddr& a = g_scratch_addr[dev];
+  const unsigned long long id = current_ctx_id();
+  if (a.ptr && id != 0 && id == a.ctx_id) {
+    *out = a.ptr;
+    return cudaSuccess;
   }
-  if (threadIdx.x == 0) out[col] = scale * sm[0];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_spectrum_scratch);
+  if (e != cudaSuccess) return e;
+  if (!p) return cudaErrorInvalidSymbol;
+  a.ptr = static_cast<double*>(p);
+  a.ctx_id = current_ctx_id();   // the lookup made the primary context current if none was
+  *out = a.ptr;
+  return cudaSuccess;
 }
 
 }  // namespace
@@ -77,18 +107,10 @@ extern "C" int vk_spectrum_noalloc(const void* u_hat, int32_t n, double l, int32
     return VK_ERR_CUDA;
   }
   double* scratch = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_spectrum_scratch);
-      if (e != cudaSuccess || !p) {
-        vk::set_global_error(cudaGetErrorString(e));
-        return VK_ERR_CUDA;
-      }
-      g_scratch_addr[dev] = static_cast<double*>(p);
-    }
-    scratch = g_scratch_addr[dev];
+  e = scratch_address(dev, &scratch);
+  if (e != cudaSuccess) {
+    vk::set_global_error(cudaGetErrorString(e));
+    return VK_ERR_CUDA;
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t cs = (size_t)n * n * (n / 2 + 1);
@@ -102,9 +124,11 @@ extern "C" int vk_spectrum_noalloc(const void* u_hat, int32_t n, double l, int32
     vk::set_global_error(cudaGetErrorString(e));
     return VK_ERR_CUDA;
   }
+  // the Neumaier-compensated column sum of vk_spectrum with the 1/2 and 1/N^6
+  // of spectrum.rs:53 folded in; every partial row is rewritten by each call,
+  // so the shared scratch needs no clearing between calls
   const double ntot = (double)n * (double)n * (double)n;
-  k_noalloc_spectrum_finish<<<nsh, 256, 0, s>>>(scratch, kNoallocBlocks, nsh, 0.5 / (ntot * ntot), spectrum_out);
-  e = cudaGetLastError();
+  e = vk::launch_reduce_columns(scratch, kNoallocBlocks, nsh, spectrum_out, s, 0.5 / (ntot * ntot));
   if (e != cudaSuccess) {
     vk::set_global_error(cudaGetErrorString(e));
     return VK_ERR_CUDA;

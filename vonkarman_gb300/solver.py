@@ -321,6 +321,42 @@ def compute_nonlinear(solver: Periodic3D, u_hat):
     return outs
 
 
+@dataclass
+class SpectralOps:
+    """The public fields of ``SpectralOps`` (vonkarman-core/src/spectral_ops.rs:10-22),
+    as the GPU forms them: ``kx``, ``ky`` (n), ``kz`` (n//2+1), ``k_mag_sq``
+    ((n, n, n//2+1)), bit-identical to ``SpectralOps::new``."""
+
+    kx: np.ndarray
+    ky: np.ndarray
+    kz: np.ndarray
+    k_mag_sq: np.ndarray
+    grid: GridSpec
+
+
+def spectral_ops(solver: Periodic3D) -> SpectralOps:
+    """``SpectralOps`` of the solver's grid (spectral_ops.rs:26-74)."""
+    lib = solver._lib
+    n = solver.grid.n
+    kx, ky, kz = np.empty(n), np.empty(n), np.empty(n // 2 + 1)
+    k2 = np.empty(solver.grid.spectral_shape)
+    nat.check(lib.vk_wavenumbers(solver._ctx, nat.dptr(kx), nat.dptr(ky), nat.dptr(kz), nat.dptr(k2)), lib,
+              solver._ctx)
+    return SpectralOps(kx, ky, kz, k2, solver.grid)
+
+
+def apply_viscous(solver: Periodic3D, u_hat, nu: float):
+    """``SpectralOps::apply_viscous`` (spectral_ops.rs:154-175): -(nu |k|^2) u_hat
+    per component, on the GPU in the solver's precision."""
+    lib = solver._lib
+    shp = solver.grid.spectral_shape
+    ins = [_as_c128(c, shp) for c in u_hat]
+    outs = [np.empty(shp, dtype=np.complex128) for _ in range(3)]
+    nat.check(lib.vk_apply_viscous_host(solver._ctx, float(nu), *[nat.dptr(c) for c in ins],
+                                        *[nat.dptr(c) for c in outs]), lib, solver._ctx)
+    return outs
+
+
 def nonlinear_adjoint(solver: Periodic3D, x, nbar):
     """N'(x)^T nbar in the raw Euclidean inner product of the stored entries."""
     lib = solver._lib

@@ -271,7 +271,7 @@ def run_reference(args, d: Dist):
     t0 = time.perf_counter()
     for i in range(1, args.steps + 1):
         s.step(1)
-        if args.spectrum_every > 0 and i % args.spectrum_every == 0:
+        if args.spectrum_every > 0 and (args.warmup + i) % args.spectrum_every == 0:
             s.spectrum()
     el = time.perf_counter() - t0
     v = args.steps / el
@@ -313,18 +313,23 @@ def pinned_like(lib, shape):
 
 
 def timed_run(s, steps: int, spec_every: int):
-    """steps ETD-RK4 steps with E(k) every spec_every steps, device-timed with
-    CUDA events on the solver's stream."""
+    """steps ETD-RK4 steps with E(k) after every step whose count is a
+    multiple of spec_every (accumulated inside that step's final stage),
+    device-timed with CUDA events on the solver's stream."""
     from vonkarman_gb300 import energy_spectrum
 
+    s.set_fused_diagnostics(0, spec_every)
+    start = s.step_count()
     s.event_mark(0)
     done = 0
     specs = 0
     while done < steps:
-        k = min(spec_every, steps - done) if spec_every > 0 else steps - done
+        k = steps - done
+        if spec_every > 0:
+            k = min(k, spec_every - (start + done) % spec_every)
         s.step(k)
         done += k
-        if spec_every > 0 and done % spec_every == 0:
+        if spec_every > 0 and (start + done) % spec_every == 0:
             energy_spectrum(s)
             specs += 1
     s.event_mark(1)

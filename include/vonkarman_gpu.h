@@ -161,6 +161,16 @@ int vk_max_vorticity(vk_ctx* ctx, double* out);
 int vk_run(vk_ctx* ctx, int64_t nsteps, int64_t every, vk_tier1_out* out, int64_t max_records,
            int64_t* n_records);
 
+/* Diagnostics fused into the step (no reference counterpart; the reference
+ * recomputes them from the state, solver.rs:412-535, spectrum.rs:13-60): on
+ * every step whose step count is a multiple of tier1_every (spectrum_every)
+ * the final stage also accumulates the Tier-1 sums (the shell spectrum) of
+ * the new state, and vk_tier1 (vk_spectrum) on that state adds those partials
+ * instead of reading the state again.  0 disables; vk_run always fuses the
+ * Tier-1 sums of its record steps.  The fused sums equal the separate ones to
+ * rounding (same per-mode terms, a different summation order). */
+int vk_set_fused_diagnostics(vk_ctx* ctx, int64_t tier1_every, int64_t spectrum_every);
+
 /* energy_spectrum (vonkarman-diag/src/spectrum.rs:13-60): shells[i] = i,
  * spectrum[i] = E(i), n = ceil(sqrt(3) * N/2) + 1 entries. */
 int vk_spectrum_len(const vk_ctx* ctx, int32_t* n);

@@ -368,9 +368,13 @@ def test_restart_bitwise(vk):
 
 
 def test_run_records_match_tier1(vk):
+    """vk_run's records (Tier-1 sums fused into the final stage of each record
+    step) against vk_tier1's separate pass over the same states: the same
+    per-mode terms summed in another order, so equal to rounding; the state,
+    time, dt and max|omega| are bitwise equal."""
     n = 16
     g = vo.Grid(n)
-    u0 = vo.taylor_green(g)
+    u0 = vo.hermitian_clean(g, vo.random_field(g, 6, amp=200.0))
     a = vk.Periodic3D(vk.GridSpec(n), 0.01, u0)
     recs = a.run(6, every=2)
     b = vk.Periodic3D(vk.GridSpec(n), 0.01, u0)
@@ -378,8 +382,37 @@ def test_run_records_match_tier1(vk):
         b.step(2)
         t = b.tier1()
         assert r.step == t.step
-        for k in ("time", "dt", "energy", "enstrophy", "helicity", "superhelicity", "max_vorticity"):
+        for k in ("time", "dt", "max_vorticity"):
             assert getattr(r, k) == getattr(t, k), k
+        for k in ("energy", "enstrophy", "helicity", "superhelicity"):
+            scale = math.sqrt(t.energy * t.enstrophy) if "helicity" in k else abs(getattr(t, k))
+            assert abs(getattr(r, k) - getattr(t, k)) <= 1e-13 * max(scale, 1e-300), k
+    assert all(np.array_equal(x, y) for x, y in zip(a.u_hat(), b.u_hat()))
+
+
+@pytest.mark.parametrize("precision,n", [("fp64", 32), ("fp32bulk", 32), ("fp32bulk", 64)])
+def test_fused_diagnostics_match_separate_passes(vk, precision, n):
+    """Tier-1 sums and E(k) accumulated inside the final stage of a step
+    (vk_set_fused_diagnostics) against the separate reduction passes over the
+    same state: equal to rounding of the FP64 sums."""
+    g = vo.Grid(n, 2.0 * math.pi if n == 64 else 3.0)
+    u0 = vo.hermitian_clean(g, vo.random_field(g, 14, amp=float(n) ** 3 / 30.0))
+    opts = vk.SolverOptions(precision=precision)
+    a = vk.Periodic3D(vk.GridSpec(n, g.l), 0.01, u0, opts)
+    b = vk.Periodic3D(vk.GridSpec(n, g.l), 0.01, u0, opts)
+    a.set_fused_diagnostics(1, 2)
+    for step in range(1, 5):
+        a.step(1)
+        b.step(1)
+        ta, tb = a.tier1(), b.tier1()
+        for k in ("energy", "enstrophy", "helicity", "superhelicity", "max_vorticity"):
+            scale = math.sqrt(tb.energy * tb.enstrophy) if "helicity" in k else abs(getattr(tb, k))
+            assert abs(getattr(ta, k) - getattr(tb, k)) <= 1e-13 * scale, (step, k)
+        sa, sb = vk.energy_spectrum(a)[1], vk.energy_spectrum(b)[1]
+        assert np.abs(sa - sb).max() <= 1e-13 * sb.max(), step
+    assert all(np.array_equal(x, y) for x, y in zip(a.u_hat(), b.u_hat()))
+    a.close()
+    b.close()
 
 
 @pytest.mark.parametrize("integrator,variant", [("rk4", "reference"), ("etd-rk4", "cox-matthews")])

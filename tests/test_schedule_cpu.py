@@ -34,8 +34,13 @@ def test_treeverse_reverses_every_step_within_slots_and_sweeps(checker):
     for (nsteps, nsnap), line in zip(CASES, out):
         f = line.split()
         assert f[0] == "ok", line
-        adv, slots, r = int(f[2]), int(f[3]), int(f[4])
+        adv, slots, r, adv_pre, spine_last = int(f[2]), int(f[3]), int(f[4]), int(f[5]), int(f[6])
         assert slots <= nsnap
         assert nsnap == 1 or math.comb(nsnap - 1 + r, r) >= nsteps
         # every step is advanced at most r times in the reversal sweeps
         assert adv <= r * nsteps, (nsteps, nsnap, adv, r)
+        # with the first descent stored by the forward run, the reversal skips
+        # exactly the advances that reached its last checkpoint
+        assert adv_pre == adv - spine_last, (nsteps, nsnap, adv, adv_pre, spine_last)
+        if nsnap > 1 and nsteps > 1:
+            assert spine_last >= 1

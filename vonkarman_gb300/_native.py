@@ -67,6 +67,7 @@ SIGNATURES = {
     "vk_superhelicity": (c_int, [_CTX, _DP]),
     "vk_max_vorticity": (c_int, [_CTX, _DP]),
     "vk_run": (c_int, [_CTX, c_int64, c_int64, POINTER(VkTier1), c_int64, POINTER(c_int64)]),
+    "vk_set_fused_diagnostics": (c_int, [_CTX, c_int64, c_int64]),
     "vk_spectrum_len": (c_int, [_CTX, POINTER(c_int32)]),
     "vk_spectrum": (c_int, [_CTX, _DP, _DP, c_int32]),
     "vk_nonlinear_host": (c_int, [_CTX, _DP, _DP, _DP, _DP, _DP, _DP]),

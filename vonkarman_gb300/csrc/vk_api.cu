@@ -161,6 +161,11 @@ struct vk_ctx {
   int red_blocks = 0;
   int n_shells = 0;
   double* dspec = nullptr;
+  // diagnostics fused into the final stage of a step (partial rows of k_p5)
+  double* dpart = nullptr;
+  int dpart_rows = 0;
+  int diag_valid = 0;                 // DiagBits the rows hold for the current state
+  int64_t fuse_t1_every = 0, fuse_spec_every = 0;
   bool has_state = false;
   bool umax_fresh = false;   // dsc->mx.umax2 describes the current state
   uint64_t step_count = 0;
@@ -174,6 +179,7 @@ struct vk_ctx {
     int64_t nseg = 0;
     std::vector<void*> ckpt;        // state at the start of each segment
     std::vector<void*> seg;         // S[0..K], A[0..K-1], B[0..K-1], C[0..K-1]
+    std::vector<int64_t> pos;       // binomial: step index of the state in each checkpoint slot (-1: none)
     void* ub = nullptr;
     void* acc = nullptr;
     void* nb = nullptr;
@@ -239,11 +245,15 @@ vk::StageArgs<R> stage_args(vk_ctx* c, int op, void* out) {
   s.dt = &c->dsc->dt;
   s.nu = c->cfg.nu;
   s.nonfinite = &c->dsc->nonfinite;
+  s.diag = 0;
+  s.nsh = c->n_shells;
+  s.dpart = c->dpart;
+  s.ks = c->ks;
   return s;
 }
 
 template <typename R>
-cudaError_t nle_t(vk_ctx* c, const void* in, int op, void* out) {
+cudaError_t nle_t(vk_ctx* c, const void* in, int op, void* out, int diag) {
   vk::NleParams<R> p{};
   p.N = c->N;
   p.ks = c->ks;
@@ -253,12 +263,14 @@ cudaError_t nle_t(vk_ctx* c, const void* in, int op, void* out) {
   p.bufB = (C2<R>*)c->bufB;
   p.twM = (const C2<R>*)c->twM;
   p.st = stage_args<R>(c, op, out);
+  p.st.diag = diag;
   p.timer = c->prof;
   return vk::Engine<R>::nle(p, c->stream);
 }
 
-cudaError_t nle(vk_ctx* c, const void* in, int op, void* out = nullptr) {
-  return c->fp32 ? nle_t<float>(c, in, op, out) : nle_t<double>(c, in, op, out);
+// diag: DiagBits to accumulate from the new state (final stages only).
+cudaError_t nle(vk_ctx* c, const void* in, int op, void* out = nullptr, int diag = 0) {
+  return c->fp32 ? nle_t<float>(c, in, op, out, diag) : nle_t<double>(c, in, op, out, diag);
 }
 
 template <typename R>
@@ -297,9 +309,16 @@ cudaError_t etd_table(vk_ctx* c, int force) {
   return vk::launch_etd_table(c->etd, c->n_etd, c->cfg.nu, c->ks * c->ks, c->dsc, force, c->cc, c->stream);
 }
 
-// Domain::step (solver.rs:383-400).
-cudaError_t step_once(vk_ctx* c) {
+// Domain::step (solver.rs:383-400).  diag: DiagBits that the final stage
+// also accumulates from the new state, besides those of the context's fused
+// cadence (vk_set_fused_diagnostics).
+cudaError_t step_once(vk_ctx* c, int diag = 0) {
   cudaError_t e;
+  {
+    const uint64_t next = c->step_count + 1;
+    if (c->fuse_t1_every > 0 && next % (uint64_t)c->fuse_t1_every == 0) diag |= vk::DIAG_TIER1;
+    if (c->fuse_spec_every > 0 && next % (uint64_t)c->fuse_spec_every == 0) diag |= vk::DIAG_SPECTRUM;
+  }
   const bool rk4 = c->cfg.integrator == VK_INTEGRATOR_RK4;
   if (c->cfg.dt_mode == VK_DT_CFL) {
     if (!c->umax_fresh) {
@@ -325,9 +344,10 @@ cudaError_t step_once(vk_ctx* c) {
     ops[0] = vk::ST_ETD_REF_1; ops[1] = vk::ST_ETD_REF_2; ops[2] = vk::ST_ETD_REF_3; ops[3] = vk::ST_ETD_4;
   }
   for (int s = 0; s < 4; ++s) {
-    e = nle(c, s == 0 ? c->u : c->temp, ops[s]);
+    e = nle(c, s == 0 ? c->u : c->temp, ops[s], nullptr, s == 3 ? diag : 0);
     if (e != cudaSuccess) return e;
   }
+  c->diag_valid = diag;
   {
     vk::TimerScope ts(c->prof, vk::PASS_SMALL, c->stream);
     e = vk::launch_time_advance(c->dsc, c->stream);
@@ -339,9 +359,17 @@ cudaError_t step_once(vk_ctx* c) {
 }
 
 // Tier-1 sums into dsc->sums and N-grid maxima (u and omega) into dsc->mx.
+// When the step that produced the state already accumulated the sums
+// (fused), only its partial rows are added.
 cudaError_t tier1_enqueue(vk_ctx* c) {
   vk::TimerScope ts(c->prof, vk::PASS_TIER1, c->stream);
-  cudaError_t e = c->fp32
+  cudaError_t e;
+  if (c->diag_valid & vk::DIAG_TIER1) {
+    e = vk::launch_reduce_columns(c->dpart, c->dpart_rows, 4, c->dsc->sums, c->stream, 1.0, 4 + c->n_shells);
+    if (e != cudaSuccess) return e;
+    return ngrid(c, 3);
+  }
+  e = c->fp32
       ? vk::Engine<float>::tier1_partial((const float2*)c->u, c->cs, c->N, c->ks, c->part, c->red_blocks, c->stream)
       : vk::Engine<double>::tier1_partial((const double2*)c->u, c->cs, c->N, c->ks, c->part, c->red_blocks,
                                           c->stream);
@@ -439,7 +467,7 @@ void free_ctx(vk_ctx* c) {
   for (cudaEvent_t& e : c->marks)
     if (e) cudaEventDestroy(e);
   void* ptrs[] = {c->u, c->temp, c->n1, c->acc, c->bufA, c->bufB, c->twN, c->twM,
-                  c->etd, c->dsc, c->records, c->part, c->dspec};
+                  c->etd, c->dsc, c->records, c->part, c->dspec, c->dpart};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -550,6 +578,9 @@ int vk_create(const vk_config* cfg, vk_ctx** out) {
   if ((e = cudaMalloc(&c->part, (size_t)c->red_blocks * width * sizeof(double))) != cudaSuccess)
     return bail(e, "cudaMalloc(partials)");
   if ((e = cudaMalloc(&c->dspec, width * sizeof(double))) != cudaSuccess) return bail(e, "cudaMalloc(spectrum)");
+  c->dpart_rows = vk::p5_ctas(n, c->fp32);
+  if ((e = cudaMalloc(&c->dpart, (size_t)c->dpart_rows * (4 + c->n_shells) * sizeof(double))) != cudaSuccess)
+    return bail(e, "cudaMalloc(fused diagnostics)");
   *out = c;
   return VK_OK;
 }
@@ -572,6 +603,7 @@ static int init_after_upload(vk_ctx* c, bool restore, double time, uint64_t step
   h.dt = restore ? dt : (c->cfg.dt_mode == VK_DT_FIXED ? c->cfg.dt_fixed : 0.0);
   VK_CHECK(c, cudaMemcpyAsync(c->dsc, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
   c->umax_fresh = false;
+  c->diag_valid = 0;
   if (!restore && c->cfg.dt_mode == VK_DT_CFL) {
     VK_CHECK(c, ngrid(c, 1));
     VK_CHECK(c, vk::launch_cfl_update(c->dsc, dx_of(c), c->cfg.nu, c->cfg.cfl_safety, 1, c->stream));
@@ -697,8 +729,9 @@ int vk_run(vk_ctx* c, int64_t nsteps, int64_t every, vk_tier1_out* out, int64_t 
   std::vector<uint64_t> steps;
   int64_t nrec = 0;
   for (int64_t i = 1; i <= nsteps; ++i) {
-    VK_CHECK(c, step_once(c));
-    if (every > 0 && i % every == 0 && nrec < want) {
+    const bool record = every > 0 && i % every == 0 && nrec < want;
+    VK_CHECK(c, step_once(c, record ? vk::DIAG_TIER1 : 0));   // Tier-1 sums fused into the final stage
+    if (record) {
       VK_CHECK(c, tier1_enqueue(c));
       VK_CHECK(c, cudaMemcpyAsync(c->records + nrec, c->dsc, sizeof(vk::DevScalars), cudaMemcpyDeviceToDevice,
                                   c->stream));
@@ -717,6 +750,14 @@ int vk_run(vk_ctx* c, int64_t nsteps, int64_t every, vk_tier1_out* out, int64_t 
   return r;
 }
 
+int vk_set_fused_diagnostics(vk_ctx* c, int64_t tier1_every, int64_t spectrum_every) {
+  if (!c) return VK_ERR_INVALID;
+  if (tier1_every < 0 || spectrum_every < 0) return fail(c, VK_ERR_INVALID, "negative cadence");
+  c->fuse_t1_every = tier1_every;
+  c->fuse_spec_every = spectrum_every;
+  return VK_OK;
+}
+
 int vk_spectrum_len(const vk_ctx* c, int32_t* n) {
   if (!c || !n) return VK_ERR_INVALID;
   *n = c->n_shells;
@@ -730,13 +771,18 @@ int vk_spectrum(vk_ctx* c, double* shells, double* spectrum, int32_t n) {
   DeviceGuard g(c->cfg.device);
   const int nsh = c->n_shells;
   vk::TimerScope ts(c->prof, vk::PASS_SPECTRUM, c->stream);
-  cudaError_t e = c->fp32
-      ? vk::Engine<float>::spectrum_partial((const float2*)c->u, c->cs, c->N, c->ks, nsh, c->part, c->red_blocks,
-                                            c->stream)
-      : vk::Engine<double>::spectrum_partial((const double2*)c->u, c->cs, c->N, c->ks, nsh, c->part,
-                                             c->red_blocks, c->stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "spectrum_partial");
-  VK_CHECK(c, vk::launch_reduce_columns(c->part, c->red_blocks, nsh, c->dspec, c->stream));
+  if (c->diag_valid & vk::DIAG_SPECTRUM) {
+    // histogram rows accumulated by the final stage of the step that made the state
+    VK_CHECK(c, vk::launch_reduce_columns(c->dpart + 4, c->dpart_rows, nsh, c->dspec, c->stream, 1.0, 4 + nsh));
+  } else {
+    cudaError_t e = c->fp32
+        ? vk::Engine<float>::spectrum_partial((const float2*)c->u, c->cs, c->N, c->ks, nsh, c->part,
+                                              c->red_blocks, c->stream)
+        : vk::Engine<double>::spectrum_partial((const double2*)c->u, c->cs, c->N, c->ks, nsh, c->part,
+                                               c->red_blocks, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "spectrum_partial");
+    VK_CHECK(c, vk::launch_reduce_columns(c->part, c->red_blocks, nsh, c->dspec, c->stream));
+  }
   std::vector<double> h(nsh);
   VK_CHECK(c, cudaMemcpyAsync(h.data(), c->dspec, nsh * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   VK_CHECK(c, cudaStreamSynchronize(c->stream));
@@ -919,6 +965,9 @@ cudaError_t forward_step_store(vk_ctx* c, void* S, void* A, void* B, void* C, vo
 // Device executor of the binomial schedule (vk_schedule.h): states live in
 // the checkpoint slots or the working buffer; advancing runs full steps in
 // place (the last stage's epilogue reads and writes u mode by mode).
+// Each slot's step index is tracked (c->adj.pos, -1 = none; the working
+// buffer separately), so that a state the forward run already stored where
+// the schedule wants it is not recomputed.
 struct AdjBinomialEx {
   vk_ctx* c;
   void* work;
@@ -926,14 +975,18 @@ struct AdjBinomialEx {
   void* B;
   void* C;
   size_t sb;
+  int64_t work_pos = -1;
   cudaError_t err = cudaSuccess;
   void* buf(int s) const { return s < 0 ? work : c->adj.ckpt[(size_t)s]; }
+  int64_t& pos(int s) { return s < 0 ? work_pos : c->adj.pos[(size_t)s]; }
   bool ok() const { return err == cudaSuccess; }
-  void copy(int d, int s) {
-    if (ok()) err = cudaMemcpyAsync(buf(d), buf(s), sb, cudaMemcpyDeviceToDevice, c->stream);
-  }
-  void advance(int s, int64_t n) {
-    for (int64_t i = 0; i < n && ok(); ++i) err = forward_step_store(c, buf(s), A, B, C, buf(s));
+  void place(int d, int s, int64_t n) {
+    const int64_t target = pos(s) + n;
+    if (d == s && n == 0) return;
+    if (pos(d) == target && pos(s) >= 0) return;
+    if (ok() && d != s) err = cudaMemcpyAsync(buf(d), buf(s), sb, cudaMemcpyDeviceToDevice, c->stream);
+    for (int64_t i = 0; i < n && ok(); ++i) err = forward_step_store(c, buf(d), A, B, C, buf(d));
+    pos(d) = ok() ? target : -1;
   }
   void reverse_step(int s) {
     if (ok()) err = forward_step_store(c, buf(s), A, B, C, nullptr);
@@ -983,8 +1036,22 @@ int vk_adjoint_forward(vk_ctx* c, int64_t nsteps, int32_t nsnap, double* J) {
   a.used = binomial ? VK_ADJ_BINOMIAL : VK_ADJ_TWO_LEVEL;
   const size_t sb = state_bytes(c);
   if (binomial) {
+    // slot 0 holds the initial state; the states of the reversal's first
+    // descent are stored as the run passes them
+    const auto spine = vk::treeverse_spine(nsteps, nsnap);
+    a.pos.assign((size_t)nsnap, -1);
     VK_CHECK(c, cudaMemcpyAsync(a.ckpt[0], c->u, sb, cudaMemcpyDeviceToDevice, c->stream));
-    for (int64_t j = 0; j < nsteps; ++j) VK_CHECK(c, step_once(c));
+    a.pos[0] = 0;
+    size_t next = 0;
+    for (int64_t j = 0; j < nsteps; ++j) {
+      if (next < spine.size() && spine[next].second == j) {
+        const int slot = spine[next].first;
+        VK_CHECK(c, cudaMemcpyAsync(a.ckpt[(size_t)slot], c->u, sb, cudaMemcpyDeviceToDevice, c->stream));
+        a.pos[(size_t)slot] = j;
+        ++next;
+      }
+      VK_CHECK(c, step_once(c));
+    }
   } else {
     for (int64_t s = 0; s < nseg; ++s) {
       VK_CHECK(c, cudaMemcpyAsync(a.ckpt[(size_t)s], c->u, sb, cudaMemcpyDeviceToDevice, c->stream));

@@ -9,9 +9,16 @@
 
 #include "vk_adjoint.cuh"
 #include "vk_lines.cuh"
+#include "vk_p3f.cuh"
 #include "vk_reduce.cuh"
 
 namespace vk {
+
+// column pairs per CTA of the fused FP32 P3 (k_p3f)
+#ifndef VK_P3F_CP
+#define VK_P3F_CP 4
+#endif
+constexpr int P3F_CP = VK_P3F_CP;
 
 // Per-device cache of the dynamic shared memory opt-in (one bit per device
 // below 64, one cache per kernel instance).  Kernels with static shared
@@ -88,8 +95,20 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     e = launch_lines<R, M, true>(o, M, p.twM, s);
     if (e != cudaSuccess) return e;
   }
-  // P3
-  {
+  // P3 (FP32 at M = 384: the fused inverse-last / cross / forward-first kernel)
+  if constexpr (sizeof(R) == 4 && M == 384) {
+    TimerScope ts(p.timer, PASS_P3, s);
+    constexpr int CP = P3F_CP;
+    const size_t smem = (size_t)P3F<CP>::SMEM_ELEMS * sizeof(float2);
+    constexpr auto kern = k_p3f<CP>;
+    e = prepare_kernel<kern>(smem);
+    if (e != cudaSuccess) return e;
+    P3Args<R> a{M * M, p.bufB, fsB2, p.bufA, fsA3};
+    const int nb = (M * M + 2 * CP - 1) / (2 * CP);
+    kern<<<nb, P3F<CP>::NT, smem, s>>>(a, p.twM);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  } else {
     TimerScope ts(p.timer, PASS_P3, s);
     constexpr int CP = zpairs<M, 384>();
     constexpr int NT = p3_threads<R, M, CP>();
@@ -110,20 +129,29 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     e = launch_lines<R, M, false>(o, M, p.twM, s);
     if (e != cudaSuccess) return e;
   }
-  // P5
+  // P5 (the DIAG instance when the stage also feeds fused diagnostics)
   {
     TimerScope ts(p.timer, PASS_P5, s);
     constexpr int NL = P5Lines<R>::value;
     constexpr int NT = p5_threads<R, M, NL>();
     const int nlines = N * H;
-    const size_t smem = (size_t)(rsmem_elems<R, M, NL>() + 3 * N * NL) * sizeof(C2<R>);
-    constexpr auto kern = k_p5<R, M, NL, NT>;
-    e = prepare_kernel<kern>(smem);
-    if (e != cudaSuccess) return e;
+    const bool diag = p.st.diag != 0;
+    const size_t smem = (size_t)(rsmem_elems<R, M, NL>() + 3 * N * NL) * sizeof(C2<R>) +
+                        (diag ? (size_t)p.st.nsh * sizeof(double) : 0);
     const double scale = (double)M * M * M / ((double)N * N * N);
     P5Args<R> a{N, M, H, nlines, (R)(1.0 / scale), ks, p.bufB, fsB4, p.st};
     const int ntiles = (nlines + NL - 1) / NL;
-    kern<<<ntiles, NT, smem, s>>>(a, p.twM);
+    if (diag) {
+      constexpr auto kern = k_p5<R, M, NL, NT, true>;
+      e = prepare_kernel<kern>(smem);
+      if (e != cudaSuccess) return e;
+      kern<<<ntiles, NT, smem, s>>>(a, p.twM);
+    } else {
+      constexpr auto kern = k_p5<R, M, NL, NT, false>;
+      e = prepare_kernel<kern>(smem);
+      if (e != cudaSuccess) return e;
+      kern<<<ntiles, NT, smem, s>>>(a, p.twM);
+    }
     e = cudaGetLastError();
   }
   return e;

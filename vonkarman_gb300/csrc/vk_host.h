@@ -63,7 +63,21 @@ template <typename R> struct StageArgs {
   const double* dt;                // device scalar
   double nu;
   int* nonfinite;                  // set when a final stage writes a non-finite value (null: no check)
+  // Diagnostics fused into a final stage (ST_ETD_4 / ST_RK4_4): bit 0 = the
+  // four Tier-1 sums, bit 1 = the shell spectrum of the new state, one row of
+  // 4 + nsh doubles per CTA of the pass in dpart (0 / null: none).
+  int diag;
+  int nsh;
+  double* dpart;
+  double ks;                       // 2 pi / L (shells of boxes other than 2 pi)
 };
+
+// Modes per CTA of the final pass (k_p5: N / 2 + 1 consecutive z per x line,
+// lines tiled by this many) and its CTA count, which sizes the fused
+// diagnostics' partial rows.
+inline int p5_lines(bool fp32) { return fp32 ? 8 : 4; }
+inline int p5_ctas(int n, bool fp32) { return (n * (n / 2 + 1) + p5_lines(fp32) - 1) / p5_lines(fp32); }
+enum DiagBits : int { DIAG_TIER1 = 1, DIAG_SPECTRUM = 2 };
 
 // Per-pass timing hook (profiling mode): brackets each kernel launch with
 // CUDA events on the launching stream.  Pass ids follow enum Pass.
@@ -165,7 +179,7 @@ cudaError_t launch_cfl_update(DevScalars* d, double dx, double nu, double safety
 cudaError_t launch_reset_max(DevScalars* d, cudaStream_t s);
 cudaError_t launch_time_advance(DevScalars* d, cudaStream_t s);
 cudaError_t launch_reduce_columns(const double* part, int nblk, int width, double* out, cudaStream_t s,
-                                  double scale = 1.0);
+                                  double scale = 1.0, int ld = 0);
 // |k|^2 of every mode of an (n, n, n/2+1) grid (SpectralOps::k_mag_sq) and
 // SpectralOps::apply_viscous on a device vector field (fp32: float2 data).
 cudaError_t launch_k_mag_sq(double* out, int n, double ks, cudaStream_t s);

@@ -231,9 +231,11 @@ __device__ __forceinline__ void flag_nonfinite(const StageArgs<R>& s, C2<R> v) {
 // components are loaded before any result is stored (a store may alias a
 // later load as far as the compiler knows, so interleaving them would
 // serialise the loads).  ok[q] = false skips mode q.
-template <typename R, int NM>
+// KEEP: the final stages (ST_ETD_4, ST_RK4_4) also return the new state of
+// each mode in un[q][c] (for diagnostics fused into the same pass).
+template <typename R, int NM, bool KEEP = false>
 __device__ __forceinline__ void stage_apply_n(const StageArgs<R>& s, const size_t* idx, const int* m, const R* k2,
-                                              const C2<R> (*nl)[3], const bool* ok) {
+                                              const C2<R> (*nl)[3], const bool* ok, C2<R> (*un)[3] = nullptr) {
   const size_t cs = s.cs;
   if (s.op == ST_NL_OUT) {
 #pragma unroll
@@ -281,9 +283,10 @@ __device__ __forceinline__ void stage_apply_n(const StageArgs<R>& s, const size_
           s.temp[i] = cmk<R>(u[q][c].x + h * rhs.x, u[q][c].y + h * rhs.y);
         } else {
           const R sixth = (R)(dt / 6.0);
-          const C2<R> un = cmk<R>(u[q][c].x + sixth * (a[q][c].x + rhs.x), u[q][c].y + sixth * (a[q][c].y + rhs.y));
-          s.u[i] = un;
-          flag_nonfinite<R>(s, un);
+          const C2<R> v = cmk<R>(u[q][c].x + sixth * (a[q][c].x + rhs.x), u[q][c].y + sixth * (a[q][c].y + rhs.y));
+          s.u[i] = v;
+          flag_nonfinite<R>(s, v);
+          if constexpr (KEEP) un[q][c] = v;
         }
       }
     }
@@ -372,9 +375,10 @@ __device__ __forceinline__ void stage_apply_n(const StageArgs<R>& s, const size_
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const C2<R> rhs = cmk<R>(a[q][c].x + b4[q] * nl[q][c].x, a[q][c].y + b4[q] * nl[q][c].y);
-          const C2<R> un = axpby<R>(ef[q], u[q][c], (R)dt, rhs);
-          s.u_out[c * cs + idx[q]] = un;
-          flag_nonfinite<R>(s, un);
+          const C2<R> v = axpby<R>(ef[q], u[q][c], (R)dt, rhs);
+          s.u_out[c * cs + idx[q]] = v;
+          flag_nonfinite<R>(s, v);
+          if constexpr (KEEP) un[q][c] = v;
         }
       }
       break;

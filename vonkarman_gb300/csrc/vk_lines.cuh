@@ -22,6 +22,7 @@
 #include <type_traits>
 
 #include "vk_kernels.cuh"
+#include "vk_reduce.cuh"
 
 namespace vk {
 
@@ -350,6 +351,7 @@ template <typename R> struct P5Args {
 };
 
 template <typename R> struct P5Lines { static constexpr int value = sizeof(R) == 8 ? 4 : 8; };
+static_assert(P5Lines<float>::value == 8 && P5Lines<double>::value == 4, "p5_lines() in vk_host.h");
 // Threads of k_p5: one butterfly per thread in the widest FFT stage; FP32 up
 // to 384 points doubles them (measured 4 % faster at 384: the epilogue keeps
 // the same modes in flight per CTA with one mode per thread, and twice the
@@ -363,7 +365,12 @@ __host__ __device__ constexpr int p5_min_blocks() {
   return NT >= 2 * rthreads<R, L, NLINES>() ? 2 : lines_min_blocks<R, L, NT, true>();
 }
 
-template <typename R, int L, int NLINES, int NT>
+// DIAG: the instance for final stages whose new state also feeds the fused
+// diagnostics (a.st.diag bits): per thread FP64 sums of the Tier-1 terms and a
+// per-CTA FP64 shell histogram in shared memory (nsh doubles after the FFT
+// buffers), written as row blockIdx.x of a.st.dpart; the rows are added by the
+// Neumaier column reduction, as the separate reduction passes do.
+template <typename R, int L, int NLINES, int NT, bool DIAG = false>
 __global__ void __launch_bounds__(NT, p5_min_blocks<R, L, NLINES, NT>())
 k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int N = 2 * L / 3;
@@ -374,6 +381,15 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   C2<R>* keep = xb + rsmem_elems<R, L, NLINES>();   // 3 fields x N x NLINES
   constexpr int H = N / 2 + 1;   // a.H of the launch
+  double* hist = reinterpret_cast<double*>(keep + 3 * N * NLINES);   // DIAG: nsh shells
+  const bool d_t1 = DIAG && (a.st.diag & DIAG_TIER1);
+  const bool d_sp = DIAG && (a.st.diag & DIAG_SPECTRUM);
+  if constexpr (DIAG) {
+    if (d_sp)
+      for (int i = threadIdx.x; i < a.st.nsh; i += NT) hist[i] = 0.0;   // ordered by the FFTs' barriers
+  }
+  double dsum[4] = {0.0, 0.0, 0.0, 0.0};
+  const bool ks_one = a.st.ks == 1.0;
   {
     const int lam = blockIdx.x * NLINES + (int)(threadIdx.x % NLINES);
     const bool ok = lam < a.nlines;
@@ -403,6 +419,7 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
     R kk[EM];
     C2<R> nl[EM][3];
     bool ok[EM];
+    int kxq[EM], kyq[EM], kzq[EM];
 #pragma unroll
     for (int q = 0; q < EM; ++q) {
       const int e = e0 + q * NT;
@@ -429,8 +446,51 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
       kk[q] = k2;
       mm[q] = kxi * kxi + kyi * kyi + z * z;
       idx[q] = ((size_t)(ok[q] ? ix : 0) * N + iy) * H + z;
+      kxq[q] = kxi; kyq[q] = kyi; kzq[q] = z;
     }
-    stage_apply_n<R, EM>(a.st, idx, mm, kk, nl, ok);
+    if constexpr (!DIAG) {
+      stage_apply_n<R, EM>(a.st, idx, mm, kk, nl, ok);
+    } else {
+      C2<R> un[EM][3];
+      stage_apply_n<R, EM, true>(a.st, idx, mm, kk, nl, ok, un);
+#pragma unroll
+      for (int q = 0; q < EM; ++q) {
+        if (!ok[q]) continue;
+        const R w = (kzq[q] == 0 || kzq[q] == N / 2) ? R(1) : R(2);   // R2C weight, exact in R
+        if (d_t1) {
+          R e, en, he, sh;
+          tier1_terms<R>(a.ks * (R)kxq[q], a.ks * (R)kyq[q], a.ks * (R)kzq[q], un[q], e, en, he, sh);
+          dsum[0] += (double)(w * e); dsum[1] += (double)(w * en);
+          dsum[2] += (double)(w * he); dsum[3] += (double)(w * sh);
+        }
+        if (d_sp) {
+          const int shell = shell_of(kxq[q], kyq[q], kzq[q], a.st.ks, ks_one);
+          if (shell < a.st.nsh) atomicAdd(&hist[shell], (double)(w * spectrum_term<R>(un[q])));
+        }
+      }
+    }
+  }
+  if constexpr (DIAG) {
+    // the CTA's row: Tier-1 sums by a fixed shuffle / warp-order tree, then
+    // the shell histogram
+    __shared__ double wsum[4][NT / 32];
+    double* row = a.st.dpart + (size_t)blockIdx.x * (4 + a.st.nsh);
+    if (d_t1) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        double v = dsum[j];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) wsum[j][threadIdx.x / 32] = v;
+      }
+    }
+    __syncthreads();
+    if (d_t1 && threadIdx.x < 4) {
+      double v = 0.0;
+      for (int w = 0; w < NT / 32; ++w) v += wsum[threadIdx.x][w];
+      row[threadIdx.x] = v;
+    }
+    if (d_sp)
+      for (int i = threadIdx.x; i < a.st.nsh; i += NT) row[4 + i] = hist[i];
   }
 }
 

@@ -99,15 +99,16 @@ __global__ void k_reset_max(DevScalars* d) {
 
 __global__ void k_time_advance(DevScalars* d) { d->time += d->dt; }
 
-// Reduce part[nblk][width] column-wise in a fixed order into
-// out[width] = scale * sum (Neumaier-compensated per thread, then a fixed
-// pairwise tree).
+// Reduce the first width columns of part[nblk][ld] column-wise in a fixed
+// order into out[width] = scale * sum (Neumaier-compensated per thread, then
+// a fixed pairwise tree).
 __global__ void __launch_bounds__(RED_THREADS)
-k_reduce_columns(const double* __restrict__ part, int nblk, int width, double scale, double* __restrict__ out) {
+k_reduce_columns(const double* __restrict__ part, int nblk, int width, int ld, double scale,
+                 double* __restrict__ out) {
   __shared__ double sm[RED_THREADS];
   for (int col = blockIdx.x; col < width; col += gridDim.x) {
     Neu a = {0, 0};
-    for (int b = threadIdx.x; b < nblk; b += RED_THREADS) a.add(part[(size_t)b * width + col]);
+    for (int b = threadIdx.x; b < nblk; b += RED_THREADS) a.add(part[(size_t)b * ld + col]);
     sm[threadIdx.x] = a.val();
     __syncthreads();
     for (int s = RED_THREADS / 2; s > 0; s >>= 1) {
@@ -198,9 +199,9 @@ cudaError_t launch_time_advance(DevScalars* d, cudaStream_t s) {
 }
 
 cudaError_t launch_reduce_columns(const double* part, int nblk, int width, double* out, cudaStream_t s,
-                                  double scale) {
+                                  double scale, int ld) {
   const int nb = width < 1024 ? width : 1024;
-  k_reduce_columns<<<nb, RED_THREADS, 0, s>>>(part, nblk, width, scale, out);
+  k_reduce_columns<<<nb, RED_THREADS, 0, s>>>(part, nblk, width, ld > 0 ? ld : width, scale, out);
   return cudaGetLastError();
 }
 

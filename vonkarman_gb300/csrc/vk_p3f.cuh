@@ -1,0 +1,219 @@
+// P3 for the FP32-bulk form at M = 384 (N = 256) with the inverse's last
+// stage, the cross product and the forward's first stage fused in registers.
+//
+// Per CTA CP column pairs; six real fields ride in three packed lines per
+// column, (u_x + i u_y), (u_z + i w_x), (w_y + i w_z), the three real cross
+// product fields of a column pair in three forward lines, F0 = c_x^A + i c_y^A,
+// F1 = c_z^A + i c_z^B, F2 = c_x^B + i c_y^B (the layout k_p3 unpacks).
+// Plans: inverse {24, 16}, forward {16, 24}.  Butterfly j' of the inverse's
+// radix-16 last stage (stride NS = 24) yields positions j' + 24 r, r < 16 --
+// exactly the inputs of butterfly j' of the forward's radix-16 first stage.
+// So one thread per (column, j') transforms the three packed lines of its
+// column at j', forms u x omega at those 16 positions and runs the forward
+// first stage there; the partner column's c_z (the other half of F1) comes
+// from the neighbouring lane by shuffle, and both lanes of a pair evaluate F1
+// (each stores half of its outputs).  Shared-memory traffic per column pair
+// drops from about 41 to 23 line transfers against the unfused k_p3.
+//
+//   phase A  inverse stage 0, radix 24 (untwiddled): inputs packed from
+//            global with the Hermitian extension, 7 of 24 inputs zero padding
+//   phase B  inverse stage 1 (radix 16) + cross product + forward stage 0
+//            (radix 16), registers; writes the forward exchange
+//   phase C  forward stage 1, radix 24
+//   phase D  unpack the kept H modes of every real field and store
+//
+// Exchange layouts (complex floats; 64-bit accesses, served per half-warp):
+//   XA (inverse): line (2 pair + cc) * 3 + t at stride LPA = 408, position p
+//     at p + p / 24.  Phase A writes positions 24 j + r (index 25 j + r: 9 j
+//     mod 16 distinct over a half-warp); phase B reads j' + 24 r (index
+//     j' + 25 r) with lanes (j', cc) interleaved, and 3 LPA = 8 (mod 16)
+//     separates the two columns' banks.
+//   XF (forward, aliases XA after a barrier): line 3 pair + f at stride
+//     LPF = 412, position p at p + p / 16; 2 LPF = 8 (mod 16) separates the
+//     F0 and F2 writes of a half-warp.
+#pragma once
+
+#include "vk_lines.cuh"
+
+namespace vk {
+
+template <int CP>
+struct P3F {
+  static constexpr int M = 384;
+  static constexpr int N = 256;
+  static constexpr int H = N / 2 + 1;   // 129 kept modes
+  static constexpr int NT = 48 * CP;    // one thread per (column, j') of the fused phase
+  static constexpr int LPA = 408;
+  static constexpr int LPF = 412;
+  static constexpr int NI = 6 * CP;     // inverse lines
+  static constexpr int NF = 3 * CP;     // forward lines
+  static constexpr int SMEM_ELEMS = NI * LPA;   // >= NF * LPF
+  static_assert(NF * LPF <= NI * LPA, "forward exchange must fit in the inverse one");
+  static_assert((3 * LPA) % 16 == 8 && (2 * LPF) % 16 == 8, "bank-spreading strides");
+  __device__ __forceinline__ static int ia(int p) { return p + p / 24; }
+  __device__ __forceinline__ static int iff(int p) { return p + p / 16; }
+};
+
+// stage twiddles of both radix-16 / radix-24 twiddled stages, conflict-free
+// per-stage tables: inverse stage 1 at (r - 1) 24 + j', forward stage 1 at
+// (r - 1) 16 + j''
+constexpr int P3F_TWI = 15 * 24;
+constexpr int P3F_TWF = 23 * 16;
+
+template <int CP>
+__global__ void __launch_bounds__(P3F<CP>::NT, 2)
+k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
+  using G = P3F<CP>;
+  constexpr int M = G::M, H = G::H, NT = G::NT;
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  __shared__ float2 twi[P3F_TWI];
+  __shared__ float2 twf[P3F_TWF];
+  for (int i = threadIdx.x; i < P3F_TWI; i += NT) {
+    const int r = i / 24 + 1, j = i - (r - 1) * 24;
+    twi[i] = tw[r * j];   // W_384^(r j), stride TWS = 384 / (24 * 16) = 1
+  }
+  for (int i = threadIdx.x; i < P3F_TWF; i += NT) {
+    const int r = i / 16 + 1, j = i - (r - 1) * 16;
+    twf[i] = tw[r * j];   // TWS = 384 / (16 * 24) = 1
+  }
+  float2* X = reinterpret_cast<float2*>(vk_smem);
+  const int col0 = blockIdx.x * 2 * CP;
+
+  // ---- phase A: inverse stage 0, radix 24 over the 6 CP packed lines -------
+  // butterfly g: line l = g / 16, j = g % 16; inputs at p = j + 16 r
+#pragma unroll 1
+  for (int g = threadIdx.x; g < 6 * CP * 16; g += NT) {
+    const int l = g >> 4, j = g & 15;
+    const int pair = l / 6, cc = (l / 3) & 1, t = l % 3;
+    const int col = col0 + 2 * pair + cc;
+    const bool okc = col < a.ncols;
+    const float2* src = a.in + (size_t)col * H;
+    float2 v[24];
+    // raw loads first (memory only), positions r in [9, 15] are zero padding
+    float2 xa[24], xb[24];
+#pragma unroll
+    for (int r = 0; r < 24; ++r) {
+      const int p = j + 16 * r;
+      xa[r] = make_float2(0.f, 0.f);
+      xb[r] = make_float2(0.f, 0.f);
+      if (r >= 9 && r <= 15) continue;
+      const bool lo = p < H;
+      if (okc && (lo || p > M - H)) {
+        const int k = lo ? p : M - p;
+        xa[r] = src[(size_t)(2 * t) * a.fsin + k];
+        xb[r] = src[(size_t)(2 * t + 1) * a.fsin + k];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 24; ++r) {
+      const int p = j + 16 * r;
+      const float2 Xv = xa[r], Yv = xb[r];
+      // Z = X + i Y with the Hermitian extension; the DC's imaginary parts
+      // are dropped (the reference backend's c2r convention)
+      v[r] = p == 0 ? make_float2(Xv.x, Yv.x)
+           : p < H ? make_float2(Xv.x - Yv.y, Xv.y + Yv.x) : make_float2(Xv.x + Yv.y, Yv.x - Xv.y);
+    }
+    float2 w0[24];
+    dft<float, true, 24, false>(v, w0);
+    float2* line = X + l * G::LPA;
+#pragma unroll
+    for (int r = 0; r < 24; ++r) line[G::ia(24 * j + r)] = v[r];
+  }
+  __syncthreads();
+
+  // ---- phase B: inverse stage 1 + cross product + forward stage 0 ----------
+  const int pair = threadIdx.x / 48;
+  const int rem = threadIdx.x - 48 * pair;
+  const int jp = rem >> 1, cc = rem & 1;
+  float cx[16], cy[16], cz[16];
+  {
+    float2 z[3][16];
+    const float2* lines = X + ((2 * pair + cc) * 3) * G::LPA;
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+#pragma unroll
+      for (int r = 0; r < 16; ++r) z[t][r] = lines[t * G::LPA + G::ia(jp + 24 * r)];
+    }
+    __syncthreads();   // XA is reused for the forward exchange below
+    float2 w[16];
+#pragma unroll
+    for (int r = 1; r < 16; ++r) w[r] = twi[(r - 1) * 24 + jp];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) dft<float, true, 16, true>(z[t], w);
+    // physical values at positions jp + 24 r: (u_x, u_y), (u_z, w_x), (w_y, w_z)
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const float ux = z[0][r].x, uy = z[0][r].y, uz = z[1][r].x, wx = z[1][r].y, wy = z[2][r].x, wz = z[2][r].y;
+      cx[r] = uy * wz - uz * wy;
+      cy[r] = uz * wx - ux * wz;
+      cz[r] = ux * wy - uy * wx;
+    }
+  }
+  {
+    float2 fo[16], f1[16], w0[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const float other = __shfl_xor_sync(0xffffffffu, cz[r], 1);
+      fo[r] = make_float2(cx[r], cy[r]);
+      f1[r] = cc == 0 ? make_float2(cz[r], other) : make_float2(other, cz[r]);
+    }
+    dft<float, false, 16, false>(fo, w0);
+    dft<float, false, 16, false>(f1, w0);
+    // stage-0 outputs at positions 16 jp + r
+    float2* lo = X + (3 * pair + (cc == 0 ? 0 : 2)) * G::LPF;
+    float2* l1 = X + (3 * pair + 1) * G::LPF;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) lo[G::iff(16 * jp + r)] = fo[r];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = cc == 0 ? i : 8 + i;
+      l1[G::iff(16 * jp + r)] = cc == 0 ? f1[i] : f1[8 + i];
+    }
+  }
+  __syncthreads();
+
+  // ---- phase C: forward stage 1, radix 24 -----------------------------------
+  {
+    const int f = rem >> 4, j = rem & 15;
+    float2* line = X + (3 * pair + f) * G::LPF;
+    float2 v[24], w[24];
+#pragma unroll
+    for (int r = 0; r < 24; ++r) v[r] = line[G::iff(j + 16 * r)];
+#pragma unroll
+    for (int r = 1; r < 24; ++r) w[r] = twf[(r - 1) * 16 + j];
+    __syncthreads();   // outputs go back into the same line positions' buffer
+    dft<float, false, 24, true>(v, w);
+#pragma unroll
+    for (int r = 0; r < 24; ++r) line[G::iff(j + 16 * r)] = v[r];
+  }
+  __syncthreads();
+
+  // ---- phase D: unpack the kept H modes of each real field and store --------
+  for (int e = threadIdx.x; e < CP * 3 * H; e += NT) {
+    const int k = e % H;
+    const int f = (e / H) % 3;
+    const int pr = e / (3 * H);
+    const float2* line = X + (3 * pr + f) * G::LPF;
+    const float2 zk = line[G::iff(k)];
+    const float2 zm = line[G::iff(k == 0 ? 0 : M - k)];
+    const float2 Xv = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+    const float2 Yv = make_float2(0.5f * (zk.y + zm.y), 0.5f * (zm.x - zk.x));
+    const int ca = col0 + 2 * pr, cb = ca + 1;
+    if (f == 0) {
+      if (ca < a.ncols) {
+        a.out[(size_t)ca * H + k] = Xv;
+        a.out[a.fsout + (size_t)ca * H + k] = Yv;
+      }
+    } else if (f == 1) {
+      if (ca < a.ncols) a.out[2 * a.fsout + (size_t)ca * H + k] = Xv;
+      if (cb < a.ncols) a.out[2 * a.fsout + (size_t)cb * H + k] = Yv;
+    } else {
+      if (cb < a.ncols) {
+        a.out[(size_t)cb * H + k] = Xv;
+        a.out[a.fsout + (size_t)cb * H + k] = Yv;
+      }
+    }
+  }
+}
+
+}  // namespace vk

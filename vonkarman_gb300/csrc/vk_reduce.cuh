@@ -26,6 +26,38 @@ struct Neu {
   __device__ __forceinline__ double val() const { return s + c; }
 };
 
+// Per-mode Tier-1 terms of one mode in the working precision R: |u|^2,
+// |omega|^2, Re(u . conj omega), Re(omega . conj(i k x omega)) with
+// omega = i k x u (spectral_ops.rs:92-104, solver.rs:412-535).  Shared by the
+// separate reduction pass and the one fused into the final stage epilogue.
+template <typename R>
+__device__ __forceinline__ void tier1_terms(R kx, R ky, R kz, const C2<R>* uv, R& e, R& en, R& he, R& sh) {
+  R ur[3], ui[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { ur[c] = uv[c].x; ui[c] = uv[c].y; }
+  const R o_r[3] = {-(ky * ui[2] - kz * ui[1]), -(kz * ui[0] - kx * ui[2]), -(kx * ui[1] - ky * ui[0])};
+  const R o_i[3] = {ky * ur[2] - kz * ur[1], kz * ur[0] - kx * ur[2], kx * ur[1] - ky * ur[0]};
+  const R c_r[3] = {-(ky * o_i[2] - kz * o_i[1]), -(kz * o_i[0] - kx * o_i[2]), -(kx * o_i[1] - ky * o_i[0])};
+  const R c_i[3] = {ky * o_r[2] - kz * o_r[1], kz * o_r[0] - kx * o_r[2], kx * o_r[1] - ky * o_r[0]};
+  e = 0; en = 0; he = 0; sh = 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    e += ur[c] * ur[c] + ui[c] * ui[c];
+    en += o_r[c] * o_r[c] + o_i[c] * o_i[c];
+    he += ur[c] * o_r[c] + ui[c] * o_i[c];
+    sh += o_r[c] * c_r[c] + o_i[c] * c_i[c];
+  }
+}
+
+// |u|^2 of one mode for the shell spectrum, in R.
+template <typename R>
+__device__ __forceinline__ R spectrum_term(const C2<R>* uv) {
+  R m2 = 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) m2 += uv[c].x * uv[c].x + uv[c].y * uv[c].y;
+  return m2;
+}
+
 template <typename R, int N>
 __global__ void __launch_bounds__(RED_THREADS)
 k_tier1_partial(const C2<R>* __restrict__ u, size_t cs, double ks, double* __restrict__ part) {
@@ -38,22 +70,11 @@ k_tier1_partial(const C2<R>* __restrict__ u, size_t cs, double ks, double* __res
     const int row = idx / H;
     const int iy = row % N, ix = row / N;
     const R kx = (R)signed_k(ix, N) * kr, ky = (R)signed_k(iy, N) * kr, kz = (R)z * kr;
-    R ur[3], ui[3];
+    C2<R> uv[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) { const C2<R> v = u[c * cs + idx]; ur[c] = v.x; ui[c] = v.y; }
-    // omega = i k x u  (spectral_ops.rs:92-104)
-    const R o_r[3] = {-(ky * ui[2] - kz * ui[1]), -(kz * ui[0] - kx * ui[2]), -(kx * ui[1] - ky * ui[0])};
-    const R o_i[3] = {ky * ur[2] - kz * ur[1], kz * ur[0] - kx * ur[2], kx * ur[1] - ky * ur[0]};
-    const R c_r[3] = {-(ky * o_i[2] - kz * o_i[1]), -(kz * o_i[0] - kx * o_i[2]), -(kx * o_i[1] - ky * o_i[0])};
-    const R c_i[3] = {ky * o_r[2] - kz * o_r[1], kz * o_r[0] - kx * o_r[2], kx * o_r[1] - ky * o_r[0]};
-    R e = 0, en = 0, he = 0, sh = 0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      e += ur[c] * ur[c] + ui[c] * ui[c];
-      en += o_r[c] * o_r[c] + o_i[c] * o_i[c];
-      he += ur[c] * o_r[c] + ui[c] * o_i[c];
-      sh += o_r[c] * c_r[c] + o_i[c] * c_i[c];
-    }
+    for (int c = 0; c < 3; ++c) uv[c] = u[c * cs + idx];
+    R e, en, he, sh;
+    tier1_terms<R>(kx, ky, kz, uv, e, en, he, sh);
     const R w = (z == 0 || z == N / 2) ? R(1) : R(2);   // exact in R
     acc[0] += (double)(w * e); acc[1] += (double)(w * en); acc[2] += (double)(w * he); acc[3] += (double)(w * sh);
   }
@@ -109,9 +130,10 @@ k_spectrum_partial(const C2<R>* __restrict__ u, size_t cs, double ks, int nsh, d
     const int iy = row % N, ix = row / N;
     const int shell = shell_of(signed_k(ix, N), signed_k(iy, N), z, ks, ks_one);
     if (shell >= nsh) continue;
-    R m2 = 0;
+    C2<R> uv[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) { const C2<R> v = u[c * cs + idx]; m2 += v.x * v.x + v.y * v.y; }
+    for (int c = 0; c < 3; ++c) uv[c] = u[c * cs + idx];
+    const R m2 = spectrum_term<R>(uv);
     const R w = (z == 0 || z == N / 2) ? R(1) : R(2);   // exact in R
     atomicAdd(&hist[shell], (double)(w * m2));
   }

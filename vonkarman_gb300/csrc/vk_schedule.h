@@ -5,15 +5,21 @@
 // CPU by a simulated executor and drives the GPU adjoint in vk_api.cu.
 //
 // Executor interface (slot -1 is the executor's working state):
-//   copy(dst, src)      state of slot src into slot dst
-//   advance(slot, n)    advance the state held in slot by n steps, in place
+//   place(dst, src, n)  slot dst receives the state n steps after the one in
+//                       slot src (a copy and n steps; an executor that knows
+//                       dst already holds that state may skip both)
 //   reverse_step(slot)  the slot holds the state before step i (the step being
 //                       reversed): recompute that step's stage inputs and
 //                       apply its adjoint; the slot is left unchanged
 //   ok()                false after a failure (the schedule stops issuing)
+//
+// The forward run that precedes the reversal can store the states of the
+// schedule's first descent (spine()) as it passes them, so that the reversal
+// starts without re-advancing the chain.
 #pragma once
 
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 namespace vk {
@@ -42,6 +48,16 @@ inline int64_t binom_sweeps(int s, int64_t n) {
   return r;
 }
 
+// Steps a treeverse call over n >= 2 steps with s >= 1 free slots advances
+// before its first checkpoint: the right part [lo + m, hi) keeps s - 1 free
+// slots and r sweeps, the left part [lo, lo + m) all s slots and r - 1 sweeps
+// (Pascal's rule).
+inline int64_t treeverse_split(int s, int64_t n) {
+  const int64_t r = binom_sweeps(s, n);
+  const int64_t right = binom_capacity(s - 1, r);
+  return n - right > 1 ? n - right : 1;
+}
+
 // Reverse steps [lo, hi): the state before step lo is in slot_lo (never
 // overwritten); free_slots lists the slots this call may use.
 template <class Ex>
@@ -56,24 +72,35 @@ void treeverse(Ex& ex, int64_t lo, int64_t hi, int slot_lo, std::vector<int>& fr
   if (s == 0) {
     // no slot left: advance a working copy from lo for every step, last first
     for (int64_t i = hi - 1; i >= lo && ex.ok(); --i) {
-      ex.copy(-1, slot_lo);
-      ex.advance(-1, i - lo);
+      ex.place(-1, slot_lo, i - lo);
       ex.reverse_step(-1);
     }
     return;
   }
-  const int64_t r = binom_sweeps(s, n);
-  // the right part [lo + m, hi) keeps s - 1 free slots and r sweeps, the left
-  // part [lo, lo + m) all s slots and r - 1 sweeps (Pascal's rule)
-  const int64_t right = binom_capacity(s - 1, r);
-  const int64_t m = n - right > 1 ? n - right : 1;
+  const int64_t m = treeverse_split(s, n);
   const int t = free_slots.back();
   free_slots.pop_back();
-  ex.copy(t, slot_lo);
-  ex.advance(t, m);
+  ex.place(t, slot_lo, m);
   treeverse(ex, lo + m, hi, t, free_slots);
   free_slots.push_back(t);
   treeverse(ex, lo, lo + m, slot_lo, free_slots);
+}
+
+// The checkpoints of the first descent of treeverse(ex, 0, nsteps, 0, free)
+// with free = {nsnap - 1, ..., 1} (slot 0 holds the initial state): the
+// (slot, step) pairs it places before reversing its first step, in order.
+// A forward run that stores the state before step `step` into `slot` for each
+// of them leaves the reversal's first descent with nothing to recompute.
+inline std::vector<std::pair<int, int64_t>> treeverse_spine(int64_t nsteps, int nsnap) {
+  std::vector<std::pair<int, int64_t>> out;
+  int64_t lo = 0;
+  // the descent pops free_slots.back(): slots 1, 2, ... while the count of
+  // free slots falls from nsnap - 1
+  for (int nfree = nsnap - 1; nsteps - lo > 1 && nfree >= 1; --nfree) {
+    lo += treeverse_split(nfree, nsteps - lo);
+    out.push_back({nsnap - nfree, lo});
+  }
+  return out;
 }
 
 }  // namespace vk

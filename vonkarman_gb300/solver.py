@@ -209,6 +209,13 @@ class Periodic3D:
         self._call(self._lib.vk_get_state_host, *[nat.dptr(c) for c in out])
         return out
 
+    def set_fused_diagnostics(self, tier1_every: int = 0, spectrum_every: int = 0):
+        """Accumulate the Tier-1 sums / shell spectrum inside the final stage of
+        every step whose count is a multiple of the given cadence (0: off);
+        ``tier1()`` / ``energy_spectrum()`` on such a state then skip their own
+        pass over it."""
+        self._call(self._lib.vk_set_fused_diagnostics, int(tier1_every), int(spectrum_every))
+
     def run(self, nsteps: int, every: int = 1):
         """Advance nsteps steps, recording Tier-1 after every ``every``-th step
         (one device->host transfer at the end)."""

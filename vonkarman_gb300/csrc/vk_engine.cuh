@@ -19,6 +19,11 @@ namespace vk {
 #define VK_P3F_CP 4
 #endif
 constexpr int P3F_CP = VK_P3F_CP;
+// radix kernels of the fused z pass on packed FP32 lane pairs
+#ifndef VK_P3F_PAIR
+#define VK_P3F_PAIR 1
+#endif
+constexpr bool P3F_PAIR = VK_P3F_PAIR != 0;
 
 // Per-device cache of the dynamic shared memory opt-in (one bit per device
 // below 64, one cache per kernel instance).  Kernels with static shared
@@ -100,7 +105,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     TimerScope ts(p.timer, PASS_P3, s);
     constexpr int CP = P3F_CP;
     const size_t smem = (size_t)P3F<CP>::SMEM_ELEMS * sizeof(float2);
-    constexpr auto kern = k_p3f<CP>;
+    constexpr auto kern = k_p3f<CP, P3F_PAIR>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
     P3Args<R> a{M * M, p.bufB, fsB2, p.bufA, fsA3};

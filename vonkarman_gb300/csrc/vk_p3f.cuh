@@ -34,6 +34,7 @@
 #pragma once
 
 #include "vk_lines.cuh"
+#include "vk_pair.cuh"
 
 namespace vk {
 
@@ -60,7 +61,9 @@ struct P3F {
 constexpr int P3F_TWI = 15 * 24;
 constexpr int P3F_TWF = 23 * 16;
 
-template <int CP>
+// PAIR: the radix kernels of phases A and B run on lane pairs (vk_pair.cuh),
+// two lines per call.
+template <int CP, bool PAIR>
 __global__ void __launch_bounds__(P3F<CP>::NT, 2)
 k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
   using G = P3F<CP>;
@@ -80,44 +83,84 @@ k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
   const int col0 = blockIdx.x * 2 * CP;
 
   // ---- phase A: inverse stage 0, radix 24 over the 6 CP packed lines -------
-  // butterfly g: line l = g / 16, j = g % 16; inputs at p = j + 16 r
-#pragma unroll 1
-  for (int g = threadIdx.x; g < 6 * CP * 16; g += NT) {
-    const int l = g >> 4, j = g & 15;
-    const int pair = l / 6, cc = (l / 3) & 1, t = l % 3;
-    const int col = col0 + 2 * pair + cc;
-    const bool okc = col < a.ncols;
-    const float2* src = a.in + (size_t)col * H;
-    float2 v[24];
-    // raw loads first (memory only), positions r in [9, 15] are zero padding
-    float2 xa[24], xb[24];
+  // butterflies (line la, j) and (line la + 3 CP, j), la = tid / 16, j = tid % 16:
+  // inputs at p = j + 16 r, positions r in [9, 15] are zero padding for every j
+  {
+    const int j = threadIdx.x & 15;
+    int lines[2];
+    lines[0] = threadIdx.x >> 4;
+    lines[1] = lines[0] + 3 * CP;
+    const float2* src[2];
+    bool okc[2];
+    int fld[2];
 #pragma unroll
-    for (int r = 0; r < 24; ++r) {
-      const int p = j + 16 * r;
-      xa[r] = make_float2(0.f, 0.f);
-      xb[r] = make_float2(0.f, 0.f);
-      if (r >= 9 && r <= 15) continue;
-      const bool lo = p < H;
-      if (okc && (lo || p > M - H)) {
-        const int k = lo ? p : M - p;
-        xa[r] = src[(size_t)(2 * t) * a.fsin + k];
-        xb[r] = src[(size_t)(2 * t + 1) * a.fsin + k];
+    for (int q = 0; q < 2; ++q) {
+      const int l = lines[q];
+      const int pair = l / 6, cc = (l / 3) & 1, t = l % 3;
+      const int col = col0 + 2 * pair + cc;
+      okc[q] = col < a.ncols;
+      src[q] = a.in + (size_t)(okc[q] ? col : 0) * H;
+      fld[q] = 2 * t;
+    }
+    // Z = X + i Y with the Hermitian extension; the DC's imaginary parts are
+    // dropped (the reference backend's c2r convention)
+    auto packz = [&](int p, float2 Xv, float2 Yv) -> float2 {
+      return p == 0 ? make_float2(Xv.x, Yv.x)
+           : p < H ? make_float2(Xv.x - Yv.y, Xv.y + Yv.x) : make_float2(Xv.x + Yv.y, Yv.x - Xv.y);
+    };
+    if constexpr (PAIR) {
+      C2f2 v[24], w0[24];
+#pragma unroll
+      for (int r = 0; r < 24; ++r) {
+        const int p = j + 16 * r;
+        float2 z[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          float2 Xv = make_float2(0.f, 0.f), Yv = make_float2(0.f, 0.f);
+          const bool lo = p < H;
+          if (!(r >= 9 && r <= 15) && okc[q] && (lo || p > M - H)) {
+            const int k = lo ? p : M - p;
+            Xv = src[q][(size_t)fld[q] * a.fsin + k];
+            Yv = src[q][(size_t)(fld[q] + 1) * a.fsin + k];
+          }
+          z[q] = packz(p, Xv, Yv);
+        }
+        v[r] = cpack(z[0], z[1]);
+      }
+      dft<f2, true, 24, false>(v, w0);
+      float2* la = X + lines[0] * G::LPA;
+      float2* lb = X + lines[1] * G::LPA;
+#pragma unroll
+      for (int r = 0; r < 24; ++r) {
+        la[G::ia(24 * j + r)] = clane0(v[r]);
+        lb[G::ia(24 * j + r)] = clane1(v[r]);
+      }
+    } else {
+#pragma unroll 1
+      for (int q = 0; q < 2; ++q) {
+        float2 v[24], w0[24];
+        float2 xa[24], xb[24];
+#pragma unroll
+        for (int r = 0; r < 24; ++r) {
+          const int p = j + 16 * r;
+          xa[r] = make_float2(0.f, 0.f);
+          xb[r] = make_float2(0.f, 0.f);
+          if (r >= 9 && r <= 15) continue;
+          const bool lo = p < H;
+          if (okc[q] && (lo || p > M - H)) {
+            const int k = lo ? p : M - p;
+            xa[r] = src[q][(size_t)fld[q] * a.fsin + k];
+            xb[r] = src[q][(size_t)(fld[q] + 1) * a.fsin + k];
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 24; ++r) v[r] = packz(j + 16 * r, xa[r], xb[r]);
+        dft<float, true, 24, false>(v, w0);
+        float2* line = X + lines[q] * G::LPA;
+#pragma unroll
+        for (int r = 0; r < 24; ++r) line[G::ia(24 * j + r)] = v[r];
       }
     }
-#pragma unroll
-    for (int r = 0; r < 24; ++r) {
-      const int p = j + 16 * r;
-      const float2 Xv = xa[r], Yv = xb[r];
-      // Z = X + i Y with the Hermitian extension; the DC's imaginary parts
-      // are dropped (the reference backend's c2r convention)
-      v[r] = p == 0 ? make_float2(Xv.x, Yv.x)
-           : p < H ? make_float2(Xv.x - Yv.y, Xv.y + Yv.x) : make_float2(Xv.x + Yv.y, Yv.x - Xv.y);
-    }
-    float2 w0[24];
-    dft<float, true, 24, false>(v, w0);
-    float2* line = X + l * G::LPA;
-#pragma unroll
-    for (int r = 0; r < 24; ++r) line[G::ia(24 * j + r)] = v[r];
   }
   __syncthreads();
 
@@ -138,8 +181,24 @@ k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
     float2 w[16];
 #pragma unroll
     for (int r = 1; r < 16; ++r) w[r] = twi[(r - 1) * 24 + jp];
+    if constexpr (PAIR) {
+      // lines 0 and 1 as one lane pair (same twiddles), line 2 alone
+      C2f2 P[16], W[16];
 #pragma unroll
-    for (int t = 0; t < 3; ++t) dft<float, true, 16, true>(z[t], w);
+      for (int r = 0; r < 16; ++r) P[r] = cpack(z[0][r], z[1][r]);
+#pragma unroll
+      for (int r = 1; r < 16; ++r) W[r] = cbcast(w[r]);
+      dft<f2, true, 16, true>(P, W);
+      dft<float, true, 16, true>(z[2], w);
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        z[0][r] = clane0(P[r]);
+        z[1][r] = clane1(P[r]);
+      }
+    } else {
+#pragma unroll
+      for (int t = 0; t < 3; ++t) dft<float, true, 16, true>(z[t], w);
+    }
     // physical values at positions jp + 24 r: (u_x, u_y), (u_z, w_x), (w_y, w_z)
 #pragma unroll
     for (int r = 0; r < 16; ++r) {
@@ -150,15 +209,28 @@ k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
     }
   }
   {
-    float2 fo[16], f1[16], w0[16];
+    float2 fo[16], f1[16];
 #pragma unroll
     for (int r = 0; r < 16; ++r) {
       const float other = __shfl_xor_sync(0xffffffffu, cz[r], 1);
       fo[r] = make_float2(cx[r], cy[r]);
       f1[r] = cc == 0 ? make_float2(cz[r], other) : make_float2(other, cz[r]);
     }
-    dft<float, false, 16, false>(fo, w0);
-    dft<float, false, 16, false>(f1, w0);
+    if constexpr (PAIR) {
+      C2f2 F[16], W0[16];
+#pragma unroll
+      for (int r = 0; r < 16; ++r) F[r] = cpack(fo[r], f1[r]);
+      dft<f2, false, 16, false>(F, W0);
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        fo[r] = clane0(F[r]);
+        f1[r] = clane1(F[r]);
+      }
+    } else {
+      float2 w0[16];
+      dft<float, false, 16, false>(fo, w0);
+      dft<float, false, 16, false>(f1, w0);
+    }
     // stage-0 outputs at positions 16 jp + r
     float2* lo = X + (3 * pair + (cc == 0 ? 0 : 2)) * G::LPF;
     float2* l1 = X + (3 * pair + 1) * G::LPF;

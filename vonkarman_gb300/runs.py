@@ -72,18 +72,50 @@ def _timed_rate(solver: Periodic3D, steps: int) -> float:
     return 1000.0 * steps / ms
 
 
+def run_to_time_spectra(solver: Periodic3D, t_end: float, max_chunk: int = 200):
+    """``run_to_time`` with Tier-1 after every step, plus the shell spectrum of
+    the last state before ``t_end`` and of the first state at or past it, so
+    that E(k) can be interpolated to ``t_end`` like the Tier-1 series.
+    Returns (records, (t_a, E_a), (t_b, E_b))."""
+    from .solver import energy_spectrum
+
+    recs = []
+    while True:
+        dt = solver.dt()
+        left = t_end - solver.time()
+        k = int(0.9 * left / dt) - 1 if dt > 0 else 0
+        if k < 2:
+            break
+        recs.extend(solver.run(min(max_chunk, k), 1))
+    before = (solver.time(), energy_spectrum(solver)[1])
+    while solver.time() < t_end:
+        before = (solver.time(), energy_spectrum(solver)[1])
+        recs.extend(solver.run(1, 1))
+    after = (solver.time(), energy_spectrum(solver)[1])
+    return recs, before, after
+
+
+def _interp_spec(a, b, t):
+    (ta, ea), (tb, eb) = a, b
+    if tb <= ta:
+        return eb
+    f = (t - ta) / (tb - ta)
+    return (1.0 - f) * ea + f * eb
+
+
 def tubes(n: int = 512, nu: float = 5e-4, t_end: float = 5.0, rate_steps: int = 20, device: int = 0) -> dict:
     grid = GridSpec(n)
     u0 = ics.lamb_oseen_tubes(n, circulation=1.0, sigma=0.25, separation=1.0, eps=0.1)
     out = {"workload": f"anti-parallel Lamb-Oseen tubes N={n}, nu={nu}, adaptive CFL 0.5, to t={t_end}, "
                        "Tier-1 after every step", "forms": {}}
-    series = {}
+    series, spec_end = {}, {}
     for prec in ("fp64", "fp32bulk"):
         s = Periodic3D(grid, nu, u0, SolverOptions(precision=prec, device=device))
         t0 = time.perf_counter()
-        recs = run_to_time(s, t_end)
+        recs, sa, sb = run_to_time_spectra(s, t_end)
         wall = time.perf_counter() - t0
         series[prec] = recs
+        spec_end[prec] = _interp_spec(sa, sb, t_end)
         u_end = s.u_hat() if prec == "fp64" else None
         rate = _timed_rate(s, rate_steps)
         out["forms"][prec] = {"steps": len(recs), "t_last": recs[-1].time, "wall_s": wall,
@@ -98,6 +130,10 @@ def tubes(n: int = 512, nu: float = 5e-4, t_end: float = 5.0, rate_steps: int = 
     out["speedup_fp32bulk_over_fp64"] = f32["steps_per_s"] / f64["steps_per_s"]
     out["rel_error_at_t_end"] = {k: abs(f32[k + "_t_end"] - f64[k + "_t_end"]) / abs(f64[k + "_t_end"])
                                  for k in ("energy", "enstrophy", "max_vorticity")}
+    a, b = spec_end["fp64"], spec_end["fp32bulk"]
+    keep = a > 1e-12 * a.max()
+    out["rel_error_at_t_end"]["spectrum_max_rel_shell"] = float(np.max(np.abs(b - a)[keep] / a[keep]))
+    out["rel_error_at_t_end"]["spectrum_max_abs_over_max"] = float(np.max(np.abs(b - a)) / a.max())
     # the largest relative deviation over the run, at equal times
     a, b = series["fp64"], series["fp32bulk"]
     tt = np.array([r.time for r in a])
@@ -112,26 +148,37 @@ def tubes(n: int = 512, nu: float = 5e-4, t_end: float = 5.0, rate_steps: int = 
 
 
 def tg(n: int = 64, nu: float = 6.25e-4, dt: float = 1e-3, steps: int = 100, device: int = 0) -> dict:
+    """Both forms; the FP32-bulk form's error against the FP64 run after the
+    last step (E, enstrophy, max|omega|, per-shell E(k))."""
     from .solver import energy_spectrum
 
     grid = GridSpec(n)
     u0 = ics.taylor_green(n)
-    s = Periodic3D(grid, nu, u0, SolverOptions(dt_mode="fixed", dt_fixed=dt, device=device))
-    s.run(3, every=1)                     # warm-up (kernel set-up)
-    s.restore_state(u0, 0.0, 0, dt)
-    t0 = time.perf_counter()
-    recs = s.run(steps, every=1)
-    _, spec = energy_spectrum(s)
-    wall = time.perf_counter() - t0
-    s.restore_state(u0, 0.0, 0, dt)
-    rate = 1000.0 * steps / s.step_timed(steps)
-    last = recs[-1]
-    s.close()
-    return {"workload": f"Taylor-Green N={n}, nu={nu}, fixed dt={dt}, {steps} steps, Tier-1 every step, "
-                        f"E(k) at step {steps}, FP64",
-            "steps_per_s_with_diagnostics": steps / wall, "steps_per_s": rate,
-            "energy": last.energy, "enstrophy": last.enstrophy, "max_vorticity": last.max_vorticity,
-            "spectrum_sum": float(np.sum(spec))}
+    out = {"workload": f"Taylor-Green N={n}, nu={nu}, fixed dt={dt}, {steps} steps, Tier-1 every step, "
+                       f"E(k) at step {steps}", "forms": {}}
+    last, spec = {}, {}
+    for prec in ("fp64", "fp32bulk"):
+        s = Periodic3D(grid, nu, u0, SolverOptions(precision=prec, dt_mode="fixed", dt_fixed=dt, device=device))
+        s.run(3, every=1)                     # warm-up (kernel set-up)
+        s.restore_state(u0, 0.0, 0, dt)
+        t0 = time.perf_counter()
+        recs = s.run(steps, every=1)
+        _, spec[prec] = energy_spectrum(s)
+        wall = time.perf_counter() - t0
+        s.restore_state(u0, 0.0, 0, dt)
+        rate = 1000.0 * steps / s.step_timed(steps)
+        last[prec] = recs[-1]
+        s.close()
+        out["forms"][prec] = {"steps_per_s_with_diagnostics": steps / wall, "steps_per_s": rate,
+                              "energy": last[prec].energy, "enstrophy": last[prec].enstrophy,
+                              "max_vorticity": last[prec].max_vorticity,
+                              "spectrum_sum": float(np.sum(spec[prec]))}
+    a, b = spec["fp64"], spec["fp32bulk"]
+    keep = a > 1e-12 * a.max()
+    out["fp32bulk_rel_error"] = {k: abs(getattr(last["fp32bulk"], k) - getattr(last["fp64"], k)) /
+                                 abs(getattr(last["fp64"], k)) for k in ("energy", "enstrophy", "max_vorticity")}
+    out["fp32bulk_rel_error"]["spectrum_max_rel_shell"] = float(np.max(np.abs(b - a)[keep] / a[keep]))
+    return out
 
 
 def isotropic(n: int = 256, nu: float = 1e-3, t_end: float = 2.0, spectrum_every: int = 10,

@@ -61,105 +61,78 @@ struct P3F {
 constexpr int P3F_TWI = 15 * 24;
 constexpr int P3F_TWF = 23 * 16;
 
-// PAIR: the radix kernels of phases A and B run on lane pairs (vk_pair.cuh),
-// two lines per call.
-template <int CP, bool PAIR>
-__global__ void __launch_bounds__(P3F<CP>::NT, 2)
-k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
+// Sources of the phase-A inputs: field f (0..5) of column col, mode k.
+// Straight from global memory, or from a shared-memory copy of the CTA's
+// 2 CP columns of all six fields (k_p3s).
+struct P3SrcGlobal {
+  const float2* in;
+  size_t fs;
+  __device__ __forceinline__ float2 operator()(int f, int col, int k) const { return in[(size_t)f * fs + (size_t)col * 129 + k]; }
+};
+template <int CP>
+struct P3SrcStaged {
+  const float2* s;   // [6][2 CP][129]
+  int col0;
+  __device__ __forceinline__ float2 operator()(int f, int col, int k) const {
+    return s[(f * 2 * CP + (col - col0)) * 129 + k];
+  }
+};
+
+// One tile of 2 CP columns (col0 ...): phases A..D.  X is the exchange
+// buffer (P3F<CP>::SMEM_ELEMS); all NT threads call it; it returns after
+// phase D's stores with no barrier after them.
+template <int CP, class SRC>
+__device__ __forceinline__ void p3f_tile(const P3Args<float>& a, int col0, float2* X, const float2* twi,
+                                         const float2* twf, const SRC& src) {
   using G = P3F<CP>;
   constexpr int M = G::M, H = G::H, NT = G::NT;
-  extern __shared__ __align__(16) unsigned char vk_smem[];
-  __shared__ float2 twi[P3F_TWI];
-  __shared__ float2 twf[P3F_TWF];
-  for (int i = threadIdx.x; i < P3F_TWI; i += NT) {
-    const int r = i / 24 + 1, j = i - (r - 1) * 24;
-    twi[i] = tw[r * j];   // W_384^(r j), stride TWS = 384 / (24 * 16) = 1
-  }
-  for (int i = threadIdx.x; i < P3F_TWF; i += NT) {
-    const int r = i / 16 + 1, j = i - (r - 1) * 16;
-    twf[i] = tw[r * j];   // TWS = 384 / (16 * 24) = 1
-  }
-  float2* X = reinterpret_cast<float2*>(vk_smem);
-  const int col0 = blockIdx.x * 2 * CP;
 
   // ---- phase A: inverse stage 0, radix 24 over the 6 CP packed lines -------
-  // butterflies (line la, j) and (line la + 3 CP, j), la = tid / 16, j = tid % 16:
-  // inputs at p = j + 16 r, positions r in [9, 15] are zero padding for every j
+  // butterflies (line la, j) and (line la + 3 CP, j), la = tid / 16, j = tid % 16,
+  // as one lane pair: inputs at p = j + 16 r, positions r in [9, 15] are zero
+  // padding for every j
   {
     const int j = threadIdx.x & 15;
-    int lines[2];
+    int lines[2], cols[2], fld[2];
+    bool okc[2];
     lines[0] = threadIdx.x >> 4;
     lines[1] = lines[0] + 3 * CP;
-    const float2* src[2];
-    bool okc[2];
-    int fld[2];
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int l = lines[q];
       const int pair = l / 6, cc = (l / 3) & 1, t = l % 3;
-      const int col = col0 + 2 * pair + cc;
-      okc[q] = col < a.ncols;
-      src[q] = a.in + (size_t)(okc[q] ? col : 0) * H;
+      cols[q] = col0 + 2 * pair + cc;
+      okc[q] = cols[q] < a.ncols;
       fld[q] = 2 * t;
     }
-    // Z = X + i Y with the Hermitian extension; the DC's imaginary parts are
-    // dropped (the reference backend's c2r convention)
-    auto packz = [&](int p, float2 Xv, float2 Yv) -> float2 {
-      return p == 0 ? make_float2(Xv.x, Yv.x)
-           : p < H ? make_float2(Xv.x - Yv.y, Xv.y + Yv.x) : make_float2(Xv.x + Yv.y, Yv.x - Xv.y);
-    };
-    if constexpr (PAIR) {
-      C2f2 v[24], w0[24];
+    C2f2 v[24], w0[24];
 #pragma unroll
-      for (int r = 0; r < 24; ++r) {
-        const int p = j + 16 * r;
-        float2 z[2];
+    for (int r = 0; r < 24; ++r) {
+      const int p = j + 16 * r;
+      float2 z[2];
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          float2 Xv = make_float2(0.f, 0.f), Yv = make_float2(0.f, 0.f);
-          const bool lo = p < H;
-          if (!(r >= 9 && r <= 15) && okc[q] && (lo || p > M - H)) {
-            const int k = lo ? p : M - p;
-            Xv = src[q][(size_t)fld[q] * a.fsin + k];
-            Yv = src[q][(size_t)(fld[q] + 1) * a.fsin + k];
-          }
-          z[q] = packz(p, Xv, Yv);
-        }
-        v[r] = cpack(z[0], z[1]);
-      }
-      dft<f2, true, 24, false>(v, w0);
-      float2* la = X + lines[0] * G::LPA;
-      float2* lb = X + lines[1] * G::LPA;
-#pragma unroll
-      for (int r = 0; r < 24; ++r) {
-        la[G::ia(24 * j + r)] = clane0(v[r]);
-        lb[G::ia(24 * j + r)] = clane1(v[r]);
-      }
-    } else {
-#pragma unroll 1
       for (int q = 0; q < 2; ++q) {
-        float2 v[24], w0[24];
-        float2 xa[24], xb[24];
-#pragma unroll
-        for (int r = 0; r < 24; ++r) {
-          const int p = j + 16 * r;
-          xa[r] = make_float2(0.f, 0.f);
-          xb[r] = make_float2(0.f, 0.f);
-          if (r >= 9 && r <= 15) continue;
-          const bool lo = p < H;
-          if (okc[q] && (lo || p > M - H)) {
-            const int k = lo ? p : M - p;
-            xa[r] = src[q][(size_t)fld[q] * a.fsin + k];
-            xb[r] = src[q][(size_t)(fld[q] + 1) * a.fsin + k];
-          }
+        float2 Xv = make_float2(0.f, 0.f), Yv = make_float2(0.f, 0.f);
+        const bool lo = p < H;
+        if (!(r >= 9 && r <= 15) && okc[q] && (lo || p > M - H)) {
+          const int k = lo ? p : M - p;
+          Xv = src(fld[q], cols[q], k);
+          Yv = src(fld[q] + 1, cols[q], k);
         }
-#pragma unroll
-        for (int r = 0; r < 24; ++r) v[r] = packz(j + 16 * r, xa[r], xb[r]);
-        dft<float, true, 24, false>(v, w0);
-        float2* line = X + lines[q] * G::LPA;
-#pragma unroll
-        for (int r = 0; r < 24; ++r) line[G::ia(24 * j + r)] = v[r];
+        // Z = X + i Y with the Hermitian extension; the DC's imaginary parts
+        // are dropped (the reference backend's c2r convention)
+        z[q] = p == 0 ? make_float2(Xv.x, Yv.x)
+             : lo ? make_float2(Xv.x - Yv.y, Xv.y + Yv.x) : make_float2(Xv.x + Yv.y, Yv.x - Xv.y);
       }
+      v[r] = cpack(z[0], z[1]);
+    }
+    dft<f2, true, 24, false>(v, w0);
+    float2* la = X + lines[0] * G::LPA;
+    float2* lb = X + lines[1] * G::LPA;
+#pragma unroll
+    for (int r = 0; r < 24; ++r) {
+      la[G::ia(24 * j + r)] = clane0(v[r]);
+      lb[G::ia(24 * j + r)] = clane1(v[r]);
     }
   }
   __syncthreads();
@@ -181,7 +154,7 @@ k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
     float2 w[16];
 #pragma unroll
     for (int r = 1; r < 16; ++r) w[r] = twi[(r - 1) * 24 + jp];
-    if constexpr (PAIR) {
+    {
       // lines 0 and 1 as one lane pair (same twiddles), line 2 alone
       C2f2 P[16], W[16];
 #pragma unroll
@@ -195,9 +168,6 @@ k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
         z[0][r] = clane0(P[r]);
         z[1][r] = clane1(P[r]);
       }
-    } else {
-#pragma unroll
-      for (int t = 0; t < 3; ++t) dft<float, true, 16, true>(z[t], w);
     }
     // physical values at positions jp + 24 r: (u_x, u_y), (u_z, w_x), (w_y, w_z)
 #pragma unroll
@@ -216,7 +186,7 @@ k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
       fo[r] = make_float2(cx[r], cy[r]);
       f1[r] = cc == 0 ? make_float2(cz[r], other) : make_float2(other, cz[r]);
     }
-    if constexpr (PAIR) {
+    {
       C2f2 F[16], W0[16];
 #pragma unroll
       for (int r = 0; r < 16; ++r) F[r] = cpack(fo[r], f1[r]);
@@ -226,10 +196,6 @@ k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
         fo[r] = clane0(F[r]);
         f1[r] = clane1(F[r]);
       }
-    } else {
-      float2 w0[16];
-      dft<float, false, 16, false>(fo, w0);
-      dft<float, false, 16, false>(f1, w0);
     }
     // stage-0 outputs at positions 16 jp + r
     float2* lo = X + (3 * pair + (cc == 0 ? 0 : 2)) * G::LPF;
@@ -286,6 +252,95 @@ k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
       }
     }
   }
+}
+
+template <int CP>
+__device__ __forceinline__ void p3f_twiddles(float2* twi, float2* twf, const float2* __restrict__ tw) {
+  for (int i = threadIdx.x; i < P3F_TWI; i += P3F<CP>::NT) {
+    const int r = i / 24 + 1, j = i - (r - 1) * 24;
+    twi[i] = tw[r * j];   // W_384^(r j), stride TWS = 384 / (24 * 16) = 1
+  }
+  for (int i = threadIdx.x; i < P3F_TWF; i += P3F<CP>::NT) {
+    const int r = i / 16 + 1, j = i - (r - 1) * 16;
+    twf[i] = tw[r * j];   // TWS = 384 / (16 * 24) = 1
+  }
+}
+
+// Resident CTAs per SM requested from the compiler (caps the registers):
+// enough for 384 threads per SM by default.
+#ifndef VK_P3F_MINB
+#define VK_P3F_MINB 0
+#endif
+template <int CP>
+__host__ __device__ constexpr int p3f_min_blocks() { return VK_P3F_MINB > 0 ? VK_P3F_MINB : 384 / P3F<CP>::NT; }
+
+// One tile per CTA, inputs straight from global memory.
+template <int CP>
+__global__ void __launch_bounds__(P3F<CP>::NT, p3f_min_blocks<CP>())
+k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  __shared__ float2 twi[P3F_TWI];
+  __shared__ float2 twf[P3F_TWF];
+  p3f_twiddles<CP>(twi, twf, tw);
+  float2* X = reinterpret_cast<float2*>(vk_smem);
+  // the first barrier of the tile orders the twiddle loads before their use
+  p3f_tile<CP>(a, blockIdx.x * 2 * CP, X, twi, twf, P3SrcGlobal{a.in, a.fsin});
+}
+
+// Persistent variant: each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x,
+// ... and copies the next tile's inputs (six fields x 2 CP columns x 129
+// modes, 16-byte cp.async chunks) into the other half of a double buffer
+// while it transforms the current one, so the loads are in flight without
+// holding registers.  Requires ncols % (2 CP) == 0 (all tiles full).
+template <int CP>
+__host__ __device__ constexpr int p3s_stage_elems() { return 6 * 2 * CP * 129; }
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <int CP>
+__device__ __forceinline__ void p3s_prefetch(const P3Args<float>& a, int tile, float2* s) {
+  // per field 2 CP x 129 float2 = 129 CP chunks of 16 bytes, contiguous in
+  // global memory (columns are adjacent) and 16-byte aligned (129 x 16 bytes
+  // per column pair)
+  constexpr int CH = 129 * CP;
+  const size_t col0 = (size_t)tile * 2 * CP;
+  for (int i = threadIdx.x; i < 6 * CH; i += P3F<CP>::NT) {
+    const int f = i / CH, c = i - f * CH;
+    const float2* g = a.in + (size_t)f * a.fsin + col0 * 129 + 2 * c;
+    cp_async16(s + (size_t)f * 2 * CP * 129 + 2 * c, g);
+  }
+}
+
+template <int CP>
+__global__ void __launch_bounds__(P3F<CP>::NT, 1)
+k_p3s(P3Args<float> a, const float2* __restrict__ tw, int ntiles) {
+  extern __shared__ __align__(16) unsigned char vk_smem[];
+  __shared__ float2 twi[P3F_TWI];
+  __shared__ float2 twf[P3F_TWF];
+  p3f_twiddles<CP>(twi, twf, tw);
+  float2* X = reinterpret_cast<float2*>(vk_smem);
+  float2* S[2];
+  S[0] = X + P3F<CP>::SMEM_ELEMS;
+  S[1] = S[0] + p3s_stage_elems<CP>();
+  int tile = blockIdx.x;
+  if (tile < ntiles) p3s_prefetch<CP>(a, tile, S[0]);
+  cp_async_commit();
+  for (int it = 0; tile < ntiles; ++it, tile += gridDim.x) {
+    const int nxt = tile + gridDim.x;
+    if (nxt < ntiles) p3s_prefetch<CP>(a, nxt, S[(it + 1) & 1]);
+    cp_async_commit();
+    cp_async_wait<1>();   // this tile's group has landed (the next one may be in flight)
+    __syncthreads();
+    p3f_tile<CP>(a, tile * 2 * CP, X, twi, twf, P3SrcStaged<CP>{S[it & 1], tile * 2 * CP});
+    __syncthreads();      // X and S[it & 1] are rewritten by the next iteration
+  }
+  cp_async_wait<0>();
 }
 
 }  // namespace vk

@@ -14,16 +14,9 @@
 
 namespace vk {
 
-// column pairs per CTA of the fused FP32 P3 (k_p3f)
-#ifndef VK_P3F_CP
-#define VK_P3F_CP 2
-#endif
-constexpr int P3F_CP = VK_P3F_CP;
-// the persistent cp.async-staged variant (k_p3s) instead of k_p3f
-#ifndef VK_P3F_STAGED
-#define VK_P3F_STAGED 0
-#endif
-constexpr bool P3F_STAGED = VK_P3F_STAGED != 0;
+// column pairs per CTA of the fused FP32 P3 (k_p3f; 2 measured faster than 4)
+constexpr int P3F_CP = 2;
+
 
 // Per-device cache of the dynamic shared memory opt-in (one bit per device
 // below 64, one cache per kernel instance).  Kernels with static shared
@@ -107,25 +100,11 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     static_assert((M * M) % (2 * CP) == 0, "whole tiles");
     P3Args<R> a{M * M, p.bufB, fsB2, p.bufA, fsA3};
     const int ntiles = M * M / (2 * CP);
-    if constexpr (P3F_STAGED) {
-      const size_t smem = (size_t)(P3F<CP>::SMEM_ELEMS + 2 * p3s_stage_elems<CP>()) * sizeof(float2);
-      constexpr auto kern = k_p3s<CP>;
-      e = prepare_kernel<kern>(smem);
-      if (e != cudaSuccess) return e;
-      int dev = 0, sms = 0, per_sm = 0;
-      if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-      if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, P3F<CP>::NT, smem)) != cudaSuccess)
-        return e;
-      const int nb = std::min(ntiles, std::max(1, per_sm) * sms);
-      kern<<<nb, P3F<CP>::NT, smem, s>>>(a, p.twM, ntiles);
-    } else {
-      const size_t smem = (size_t)P3F<CP>::SMEM_ELEMS * sizeof(float2);
-      constexpr auto kern = k_p3f<CP>;
-      e = prepare_kernel<kern>(smem);
-      if (e != cudaSuccess) return e;
-      kern<<<ntiles, P3F<CP>::NT, smem, s>>>(a, p.twM);
-    }
+    const size_t smem = (size_t)P3F<CP>::SMEM_ELEMS * sizeof(float2);
+    constexpr auto kern = k_p3f<CP>;
+    e = prepare_kernel<kern>(smem);
+    if (e != cudaSuccess) return e;
+    kern<<<ntiles, P3F<CP>::NT, smem, s>>>(a, p.twM);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   } else {

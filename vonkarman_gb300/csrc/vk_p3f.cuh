@@ -61,20 +61,13 @@ struct P3F {
 constexpr int P3F_TWI = 15 * 24;
 constexpr int P3F_TWF = 23 * 16;
 
-// Sources of the phase-A inputs: field f (0..5) of column col, mode k.
-// Straight from global memory, or from a shared-memory copy of the CTA's
-// 2 CP columns of all six fields (k_p3s).
+// Source of the phase-A inputs: field f (0..5) of column col, mode k,
+// straight from global memory.
 struct P3SrcGlobal {
   const float2* in;
   size_t fs;
-  __device__ __forceinline__ float2 operator()(int f, int col, int k) const { return in[(size_t)f * fs + (size_t)col * 129 + k]; }
-};
-template <int CP>
-struct P3SrcStaged {
-  const float2* s;   // [6][2 CP][129]
-  int col0;
   __device__ __forceinline__ float2 operator()(int f, int col, int k) const {
-    return s[(f * 2 * CP + (col - col0)) * 129 + k];
+    return in[(size_t)f * fs + (size_t)col * 129 + k];
   }
 };
 
@@ -266,17 +259,9 @@ __device__ __forceinline__ void p3f_twiddles(float2* twi, float2* twf, const flo
   }
 }
 
-// Resident CTAs per SM requested from the compiler (caps the registers):
-// enough for 384 threads per SM by default.
-#ifndef VK_P3F_MINB
-#define VK_P3F_MINB 0
-#endif
-template <int CP>
-__host__ __device__ constexpr int p3f_min_blocks() { return VK_P3F_MINB > 0 ? VK_P3F_MINB : 384 / P3F<CP>::NT; }
-
 // One tile per CTA, inputs straight from global memory.
 template <int CP>
-__global__ void __launch_bounds__(P3F<CP>::NT, p3f_min_blocks<CP>())
+__global__ void __launch_bounds__(P3F<CP>::NT, 384 / P3F<CP>::NT)
 k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char vk_smem[];
   __shared__ float2 twi[P3F_TWI];
@@ -285,62 +270,6 @@ k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
   float2* X = reinterpret_cast<float2*>(vk_smem);
   // the first barrier of the tile orders the twiddle loads before their use
   p3f_tile<CP>(a, blockIdx.x * 2 * CP, X, twi, twf, P3SrcGlobal{a.in, a.fsin});
-}
-
-// Persistent variant: each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x,
-// ... and copies the next tile's inputs (six fields x 2 CP columns x 129
-// modes, 16-byte cp.async chunks) into the other half of a double buffer
-// while it transforms the current one, so the loads are in flight without
-// holding registers.  Requires ncols % (2 CP) == 0 (all tiles full).
-template <int CP>
-__host__ __device__ constexpr int p3s_stage_elems() { return 6 * 2 * CP * 129; }
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-template <int CP>
-__device__ __forceinline__ void p3s_prefetch(const P3Args<float>& a, int tile, float2* s) {
-  // per field 2 CP x 129 float2 = 129 CP chunks of 16 bytes, contiguous in
-  // global memory (columns are adjacent) and 16-byte aligned (129 x 16 bytes
-  // per column pair)
-  constexpr int CH = 129 * CP;
-  const size_t col0 = (size_t)tile * 2 * CP;
-  for (int i = threadIdx.x; i < 6 * CH; i += P3F<CP>::NT) {
-    const int f = i / CH, c = i - f * CH;
-    const float2* g = a.in + (size_t)f * a.fsin + col0 * 129 + 2 * c;
-    cp_async16(s + (size_t)f * 2 * CP * 129 + 2 * c, g);
-  }
-}
-
-template <int CP>
-__global__ void __launch_bounds__(P3F<CP>::NT, 1)
-k_p3s(P3Args<float> a, const float2* __restrict__ tw, int ntiles) {
-  extern __shared__ __align__(16) unsigned char vk_smem[];
-  __shared__ float2 twi[P3F_TWI];
-  __shared__ float2 twf[P3F_TWF];
-  p3f_twiddles<CP>(twi, twf, tw);
-  float2* X = reinterpret_cast<float2*>(vk_smem);
-  float2* S[2];
-  S[0] = X + P3F<CP>::SMEM_ELEMS;
-  S[1] = S[0] + p3s_stage_elems<CP>();
-  int tile = blockIdx.x;
-  if (tile < ntiles) p3s_prefetch<CP>(a, tile, S[0]);
-  cp_async_commit();
-  for (int it = 0; tile < ntiles; ++it, tile += gridDim.x) {
-    const int nxt = tile + gridDim.x;
-    if (nxt < ntiles) p3s_prefetch<CP>(a, nxt, S[(it + 1) & 1]);
-    cp_async_commit();
-    cp_async_wait<1>();   // this tile's group has landed (the next one may be in flight)
-    __syncthreads();
-    p3f_tile<CP>(a, tile * 2 * CP, X, twi, twf, P3SrcStaged<CP>{S[it & 1], tile * 2 * CP});
-    __syncthreads();      // X and S[it & 1] are rewritten by the next iteration
-  }
-  cp_async_wait<0>();
 }
 
 }  // namespace vk

@@ -60,7 +60,7 @@ class AscentResult:
 
 
 def enstrophy_ascent(grid: GridSpec, nu: float, dt: float, u0, nsteps: int, iters: int = 10, nsnap: int = 20,
-                     precision: str = "fp32bulk", step: float = 0.2) -> AscentResult:
+                     precision: str = "fp32bulk", step: float = 0.2, schedule: str = "two-level") -> AscentResult:
     """Projected-gradient ascent of the final enstrophy on the sphere
     <u, u> = <u0, u0>: the gradient is projected on the tangent space, the
     step length is ``step`` times the radius, and the iterate is pulled back
@@ -72,7 +72,7 @@ def enstrophy_ascent(grid: GridSpec, nu: float, dt: float, u0, nsteps: int, iter
     s = Periodic3D(grid, nu, u, SolverOptions(precision=precision, dt_mode="fixed", dt_fixed=dt))
     res = AscentResult(u=u)
     for _ in range(iters):
-        J, g = gradient(s, u, nsteps, nsnap)
+        J, g = gradient(s, u, nsteps, nsnap, schedule)
         gt = _axpy(-l2_inner(g, u, n) / r2, u, g)
         gn = math.sqrt(max(l2_inner(gt, gt, n), 0.0))
         res.J.append(J)
@@ -82,7 +82,7 @@ def enstrophy_ascent(grid: GridSpec, nu: float, dt: float, u0, nsteps: int, iter
         un = _axpy(step * math.sqrt(r2) / gn, gt, u)
         u = [c * math.sqrt(r2 / l2_inner(un, un, n)) for c in un]
     s.restore_state(u, 0.0, 0, dt)
-    res.J.append(s.adjoint_forward(nsteps, nsnap))
+    res.J.append(s.adjoint_forward(nsteps, nsnap, schedule=schedule))
     res.u = u
     s.close()
     return res

@@ -172,6 +172,22 @@ def test_nonlinear_fp32bulk_vs_fp64_n256(vk):
     assert nrel(out[1], out[0]) < TOL32
 
 
+def test_nonlinear_fp32bulk_vs_fp64_n512(vk):
+    # the 768-point plans of both forms (one column pair per CTA, z pass in
+    # place) against each other: agreement to the FP32 level
+    from vonkarman_gb300 import ics
+
+    n = 512
+    u = ics.lamb_oseen_tubes(n)
+    out = []
+    for prec in ("fp64", "fp32bulk"):
+        s = vk.Periodic3D(vk.GridSpec(n), 5e-4, u, vk.SolverOptions(precision=prec, dt_mode="fixed",
+                                                                      dt_fixed=1e-3))
+        out.append(vk.compute_nonlinear(s, u))
+        s.close()
+    assert nrel(out[1], out[0]) < TOL32
+
+
 def test_nonlinear_non_hermitian_input(vk):
     # raw random spectral data (not Hermitian in the kz=0 plane): the padded
     # c2r must drop exactly what the reference's backend drops

@@ -111,7 +111,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     TimerScope ts(p.timer, PASS_P3, s);
     constexpr int CP = zpairs<M, 384>();
     constexpr int NT = p3_threads<R, M, CP>();
-    const size_t smem = (size_t)12 * CP * zpad_len<R>(M) * sizeof(C2<R>);
+    const size_t smem = (size_t)p3_smem_lines<R, M, CP>() * zpad_len<R>(M) * sizeof(C2<R>);
     constexpr auto kern = k_p3<R, M, CP, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;

@@ -509,22 +509,36 @@ template <typename R, int M, int CP>
 __host__ __device__ constexpr int p3_threads() {
   return cmin(rthreads<R, M, 6 * CP, true>(), 384);
 }
+// One column pair per CTA (M >= 384): the inverse writes its physical values
+// in place, the cross product overwrites three of the six lines position by
+// position (each position of the pair is read and written by one thread),
+// and the forward exchanges through the other three, so the CTA needs 6
+// lines of shared memory instead of 12.
+#ifndef VK_P3_INPLACE
+#define VK_P3_INPLACE 1
+#endif
+template <int CP> __host__ __device__ constexpr bool p3_inplace() { return VK_P3_INPLACE && CP == 1; }
+template <typename R, int M, int CP>
+__host__ __device__ constexpr int p3_smem_lines() { return (p3_inplace<CP>() ? 6 : 12) * CP; }
 
 template <typename R, int M, int CP, int NT>
-__global__ void __launch_bounds__(NT, M >= 768 ? 1 : cmax(1, (sizeof(R) == 8 ? 768 : 512) / NT))
+__global__ void __launch_bounds__(NT, M >= 768 ? (sizeof(R) == 4 && p3_inplace<CP>() ? 3 : 1)
+                                              : cmax(1, (sizeof(R) == 8 ? 768 : 512) / NT))
 k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr int N = 2 * M / 3;
   constexpr int H = N / 2 + 1;
   constexpr int LP = zpad_len<R>(M);
   constexpr int NI = 6 * CP, NF = 3 * CP;
+  constexpr bool INPL = p3_inplace<CP>();
   extern __shared__ __align__(16) unsigned char vk_smem[];
   __shared__ C2<R> tw_s[twtab_elems<R, true>(M)];
   load_twtab<R, M, true, NT>(tw_s, tw);
   C2<R>* A = reinterpret_cast<C2<R>*>(vk_smem);
-  C2<R>* B = A + NI * LP;
+  C2<R>* B = INPL ? A : A + NI * LP;
+  C2<R>* XF = INPL ? A + NF * LP : B;   // exchange of the forward transform
   const int col0 = blockIdx.x * 2 * CP;
   // positions H .. M - H of the packed lines are the z zero-padding
-  fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>, false, true, H, M - H + 1>(
+  fft_lines<R, M, true, NT, NI, MapContig<R, M, NI>, INPL, true, H, M - H + 1>(
       A, tw_s,
       [&](int l, int p) -> C2x2<R> {
         const int t = l / (2 * CP);
@@ -564,7 +578,7 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
   }
   __syncthreads();
   fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>, false, true>(
-      B, tw_s, [&](int l, int p) { return A[l * LP + zi<R>(p)]; }, PrepNone{},
+      XF, tw_s, [&](int l, int p) { return A[l * LP + zi<R>(p)]; }, PrepNone{},
       [&](int l, int p, C2<R> v) { A[l * LP + zi<R>(p)] = v; });
   __syncthreads();
   for (int e = threadIdx.x; e < CP * 3 * H; e += NT) {

@@ -138,6 +138,12 @@ int vk_get_state_host(vk_ctx* ctx, double* ux, double* uy, double* uz);
 /* Domain::step (solver.rs:383-400), nsteps times, enqueued on the context's
  * stream without host synchronisation between steps. */
 int vk_step(vk_ctx* ctx, int64_t nsteps);
+/* Steps as CUDA graphs (no reference counterpart): with enable != 0 (the
+ * default) vk_step, vk_run and the adjoint forward replay each step's ~30
+ * kernel launches as one captured graph (one graph per launch sequence,
+ * captured the second time that sequence runs); results are those of the
+ * eager launches.  Profiling (vk_profile_enable) always launches eagerly. */
+int vk_use_graphs(vk_ctx* ctx, int32_t enable);
 /* Domain::time / step_count / dt (domain.rs:44-50). */
 int vk_time(vk_ctx* ctx, double* out);
 int vk_step_count(vk_ctx* ctx, uint64_t* out);

@@ -96,6 +96,7 @@ unsafe extern "C" {
     pub fn vk_restore_host(ctx: *mut vk_ctx, ux: *const f64, uy: *const f64, uz: *const f64, time: f64, step_count: u64, dt: f64) -> c_int;
     pub fn vk_get_state_host(ctx: *mut vk_ctx, ux: *mut f64, uy: *mut f64, uz: *mut f64) -> c_int;
     pub fn vk_step(ctx: *mut vk_ctx, nsteps: i64) -> c_int;
+    pub fn vk_use_graphs(ctx: *mut vk_ctx, enable: i32) -> c_int;
     pub fn vk_time(ctx: *mut vk_ctx, out_: *mut f64) -> c_int;
     pub fn vk_step_count(ctx: *mut vk_ctx, out_: *mut u64) -> c_int;
     pub fn vk_dt(ctx: *mut vk_ctx, out_: *mut f64) -> c_int;

@@ -56,6 +56,7 @@ SIGNATURES = {
     "vk_restore_host": (c_int, [_CTX, _DP, _DP, _DP, c_double, c_uint64, c_double]),
     "vk_get_state_host": (c_int, [_CTX, _DP, _DP, _DP]),
     "vk_step": (c_int, [_CTX, c_int64]),
+    "vk_use_graphs": (c_int, [_CTX, c_int32]),
     "vk_time": (c_int, [_CTX, _DP]),
     "vk_step_count": (c_int, [_CTX, POINTER(c_uint64)]),
     "vk_dt": (c_int, [_CTX, _DP]),

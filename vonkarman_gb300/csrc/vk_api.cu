@@ -166,6 +166,12 @@ struct vk_ctx {
   int dpart_rows = 0;
   int diag_valid = 0;                 // DiagBits the rows hold for the current state
   int64_t fuse_t1_every = 0, fuse_spec_every = 0;
+  // steps replayed as CUDA graphs, one per launch-sequence key (step_graph)
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    bool eager = false;
+  } graphs[8];
+  bool use_graphs = true;
   bool has_state = false;
   bool umax_fresh = false;   // dsc->mx.umax2 describes the current state
   uint64_t step_count = 0;
@@ -309,16 +315,10 @@ cudaError_t etd_table(vk_ctx* c, int force) {
   return vk::launch_etd_table(c->etd, c->n_etd, c->cfg.nu, c->ks * c->ks, c->dsc, force, c->cc, c->stream);
 }
 
-// Domain::step (solver.rs:383-400).  diag: DiagBits that the final stage
-// also accumulates from the new state, besides those of the context's fused
-// cadence (vk_set_fused_diagnostics).
-cudaError_t step_once(vk_ctx* c, int diag = 0) {
+// The kernels of one step, enqueued on the context's stream (no host-side
+// bookkeeping besides ngrid's flag, so the sequence can be captured).
+cudaError_t enqueue_step(vk_ctx* c, int diag) {
   cudaError_t e;
-  {
-    const uint64_t next = c->step_count + 1;
-    if (c->fuse_t1_every > 0 && next % (uint64_t)c->fuse_t1_every == 0) diag |= vk::DIAG_TIER1;
-    if (c->fuse_spec_every > 0 && next % (uint64_t)c->fuse_spec_every == 0) diag |= vk::DIAG_SPECTRUM;
-  }
   const bool rk4 = c->cfg.integrator == VK_INTEGRATOR_RK4;
   if (c->cfg.dt_mode == VK_DT_CFL) {
     if (!c->umax_fresh) {
@@ -347,12 +347,53 @@ cudaError_t step_once(vk_ctx* c, int diag = 0) {
     e = nle(c, s == 0 ? c->u : c->temp, ops[s], nullptr, s == 3 ? diag : 0);
     if (e != cudaSuccess) return e;
   }
-  c->diag_valid = diag;
-  {
-    vk::TimerScope ts(c->prof, vk::PASS_SMALL, c->stream);
-    e = vk::launch_time_advance(c->dsc, c->stream);
+  vk::TimerScope ts(c->prof, vk::PASS_SMALL, c->stream);
+  return vk::launch_time_advance(c->dsc, c->stream);
+}
+
+// A step as a CUDA graph: the launch sequence of a step depends only on the
+// fused-diagnostics bits and on whether the N-grid maxima of the state are
+// already known, so one graph per such key is captured (after the key has
+// run once eagerly, which performs every kernel's one-time set-up) and then
+// replayed, replacing about 30 kernel launches per step by one.
+cudaError_t step_graph(vk_ctx* c, int diag) {
+  const int key = diag | (c->cfg.dt_mode == VK_DT_CFL && c->umax_fresh ? 4 : 0);
+  vk_ctx::StepGraph& g = c->graphs[key];
+  if (g.exec) return cudaGraphLaunch(g.exec, c->stream);
+  if (!g.eager) {
+    g.eager = true;
+    return enqueue_step(c, diag);
   }
+  cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
+  const cudaError_t e_enq = enqueue_step(c, diag);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e_end = cudaStreamEndCapture(c->stream, &graph);
+  if (e_enq != cudaSuccess || e_end != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return e_enq != cudaSuccess ? e_enq : e_end;
+  }
+  e = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    g.exec = nullptr;
+    return e;
+  }
+  return cudaGraphLaunch(g.exec, c->stream);
+}
+
+// Domain::step (solver.rs:383-400).  diag: DiagBits that the final stage
+// also accumulates from the new state, besides those of the context's fused
+// cadence (vk_set_fused_diagnostics).
+cudaError_t step_once(vk_ctx* c, int diag = 0) {
+  {
+    const uint64_t next = c->step_count + 1;
+    if (c->fuse_t1_every > 0 && next % (uint64_t)c->fuse_t1_every == 0) diag |= vk::DIAG_TIER1;
+    if (c->fuse_spec_every > 0 && next % (uint64_t)c->fuse_spec_every == 0) diag |= vk::DIAG_SPECTRUM;
+  }
+  const cudaError_t e = c->use_graphs && !c->prof ? step_graph(c, diag) : enqueue_step(c, diag);
+  if (e != cudaSuccess) return e;
+  c->diag_valid = diag;
   c->step_count += 1;
   c->umax_fresh = false;
   return cudaSuccess;
@@ -458,7 +499,15 @@ void free_adjoint(vk_ctx* c) {
   c->adj = vk_ctx::Adjoint();
 }
 
+void free_graphs(vk_ctx* c) {
+  for (auto& g : c->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = vk_ctx::StepGraph();
+  }
+}
+
 void free_ctx(vk_ctx* c) {
+  free_graphs(c);
   free_adjoint(c);
   delete c->prof;
   c->prof = nullptr;
@@ -748,6 +797,15 @@ int vk_run(vk_ctx* c, int64_t nsteps, int64_t every, vk_tier1_out* out, int64_t 
   for (int64_t k = 0; k < nrec; ++k) fill_tier1(c, h[(size_t)k], steps[(size_t)k], out + k);
   if (n_records) *n_records = nrec;
   return r;
+}
+
+int vk_use_graphs(vk_ctx* c, int32_t enable) {
+  if (!c) return VK_ERR_INVALID;
+  DeviceGuard g(c->cfg.device);
+  VK_CHECK(c, cudaStreamSynchronize(c->stream));
+  c->use_graphs = enable != 0;
+  if (!c->use_graphs) free_graphs(c);
+  return VK_OK;
 }
 
 int vk_set_fused_diagnostics(vk_ctx* c, int64_t tier1_every, int64_t spectrum_every) {

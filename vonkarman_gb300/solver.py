@@ -164,6 +164,11 @@ class Periodic3D:
     def step(self, nsteps: int = 1):
         self._call(self._lib.vk_step, int(nsteps))
 
+    def use_graphs(self, enable: bool = True):
+        """Replay steps as captured CUDA graphs (the default) or launch every
+        kernel eagerly."""
+        self._call(self._lib.vk_use_graphs, 1 if enable else 0)
+
     def _scalar(self, fn) -> float:
         v = ctypes.c_double()
         self._call(fn, ctypes.byref(v))

@@ -627,7 +627,7 @@ int vk_create(const vk_config* cfg, vk_ctx** out) {
   if ((e = cudaMalloc(&c->part, (size_t)c->red_blocks * width * sizeof(double))) != cudaSuccess)
     return bail(e, "cudaMalloc(partials)");
   if ((e = cudaMalloc(&c->dspec, width * sizeof(double))) != cudaSuccess) return bail(e, "cudaMalloc(spectrum)");
-  c->dpart_rows = vk::p5_ctas(n, c->fp32);
+  c->dpart_rows = vk::p5_ctas(n, c->fp32);   // rows of k_p5 at this grid
   if ((e = cudaMalloc(&c->dpart, (size_t)c->dpart_rows * (4 + c->n_shells) * sizeof(double))) != cudaSuccess)
     return bail(e, "cudaMalloc(fused diagnostics)");
   *out = c;

@@ -131,7 +131,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   // P5 (the DIAG instance when the stage also feeds fused diagnostics)
   {
     TimerScope ts(p.timer, PASS_P5, s);
-    constexpr int NL = P5Lines<R>::value;
+    constexpr int NL = P5Lines<R, M>::value;
     constexpr int NT = p5_threads<R, M, NL>();
     const int nlines = N * H;
     const bool diag = p.st.diag != 0;

@@ -75,8 +75,11 @@ template <typename R> struct StageArgs {
 // Modes per CTA of the final pass (k_p5: N / 2 + 1 consecutive z per x line,
 // lines tiled by this many) and its CTA count, which sizes the fused
 // diagnostics' partial rows.
-inline int p5_lines(bool fp32) { return fp32 ? 8 : 4; }
-inline int p5_ctas(int n, bool fp32) { return (n * (n / 2 + 1) + p5_lines(fp32) - 1) / p5_lines(fp32); }
+#ifndef VK_P5_LINES_768
+#define VK_P5_LINES_768 8
+#endif
+inline constexpr int p5_lines(int n, bool fp32) { return fp32 ? (n >= 512 ? VK_P5_LINES_768 : 8) : 4; }
+inline constexpr int p5_ctas(int n, bool fp32) { return (n * (n / 2 + 1) + p5_lines(n, fp32) - 1) / p5_lines(n, fp32); }
 enum DiagBits : int { DIAG_TIER1 = 1, DIAG_SPECTRUM = 2 };
 
 // Per-pass timing hook (profiling mode): brackets each kernel launch with

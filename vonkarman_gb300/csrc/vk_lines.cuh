@@ -350,8 +350,9 @@ template <typename R> struct P5Args {
   StageArgs<R> st;
 };
 
-template <typename R> struct P5Lines { static constexpr int value = sizeof(R) == 8 ? 4 : 8; };
-static_assert(P5Lines<float>::value == 8 && P5Lines<double>::value == 4, "p5_lines() in vk_host.h");
+// lines per CTA of k_p5 at padded length L (the grid N = 2 L / 3), shared
+// with the host's sizing of the fused-diagnostics rows
+template <typename R, int L> struct P5Lines { static constexpr int value = p5_lines(2 * L / 3, sizeof(R) == 4); };
 // Threads of k_p5: one butterfly per thread in the widest FFT stage; FP32 up
 // to 384 points doubles them (measured 4 % faster at 384: the epilogue keeps
 // the same modes in flight per CTA with one mode per thread, and twice the

@@ -254,6 +254,7 @@ vk::StageArgs<R> stage_args(vk_ctx* c, int op, void* out) {
   s.diag = 0;
   s.nsh = c->n_shells;
   s.dpart = c->dpart;
+  s.dpart_rows = c->dpart_rows;
   s.ks = c->ks;
   return s;
 }

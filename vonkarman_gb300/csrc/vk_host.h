@@ -69,16 +69,14 @@ template <typename R> struct StageArgs {
   int diag;
   int nsh;
   double* dpart;
+  int dpart_rows;                  // rows allocated in dpart (a CTA past them writes nothing)
   double ks;                       // 2 pi / L (shells of boxes other than 2 pi)
 };
 
 // Modes per CTA of the final pass (k_p5: N / 2 + 1 consecutive z per x line,
 // lines tiled by this many) and its CTA count, which sizes the fused
 // diagnostics' partial rows.
-#ifndef VK_P5_LINES_768
-#define VK_P5_LINES_768 8
-#endif
-inline constexpr int p5_lines(int n, bool fp32) { return fp32 ? (n >= 512 ? VK_P5_LINES_768 : 8) : 4; }
+inline constexpr int p5_lines(int n, bool fp32) { return (void)n, fp32 ? 8 : 4; }
 inline constexpr int p5_ctas(int n, bool fp32) { return (n * (n / 2 + 1) + p5_lines(n, fp32) - 1) / p5_lines(n, fp32); }
 enum DiagBits : int { DIAG_TIER1 = 1, DIAG_SPECTRUM = 2 };
 

@@ -475,7 +475,8 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
     // the CTA's row: Tier-1 sums by a fixed shuffle / warp-order tree, then
     // the shell histogram
     __shared__ double wsum[4][NT / 32];
-    double* row = a.st.dpart + (size_t)blockIdx.x * (4 + a.st.nsh);
+    const bool has_row = (int)blockIdx.x < a.st.dpart_rows;
+    double* row = a.st.dpart + (size_t)(has_row ? blockIdx.x : 0) * (4 + a.st.nsh);
     if (d_t1) {
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
@@ -485,12 +486,12 @@ k_p5(P5Args<R> a, const C2<R>* __restrict__ tw) {
       }
     }
     __syncthreads();
-    if (d_t1 && threadIdx.x < 4) {
+    if (d_t1 && has_row && threadIdx.x < 4) {
       double v = 0.0;
       for (int w = 0; w < NT / 32; ++w) v += wsum[threadIdx.x][w];
       row[threadIdx.x] = v;
     }
-    if (d_sp)
+    if (d_sp && has_row)
       for (int i = threadIdx.x; i < a.st.nsh; i += NT) row[4 + i] = hist[i];
   }
 }

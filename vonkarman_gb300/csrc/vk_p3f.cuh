@@ -82,12 +82,13 @@ __device__ __forceinline__ void p3f_tile(const P3Args<float>& a, int col0, float
 
   // ---- phase A: inverse stage 0, radix 24 over the 6 CP packed lines -------
   // butterflies (line la, j) and (line la + 3 CP, j), la = tid / 16, j = tid % 16,
-  // as one lane pair: inputs at p = j + 16 r, positions r in [9, 15] are zero
-  // padding for every j
+  // as one lane pair.  Inputs at p = j + 16 r: r <= 7 are kept modes k = p, r = 8
+  // is the mode k = 128 for j = 0 and padding otherwise, r in [9, 15] padding,
+  // r >= 16 the Hermitian mirror k = M - p (tiles are always full: 2 CP divides
+  // M^2, so no column bound is checked).
   {
     const int j = threadIdx.x & 15;
     int lines[2], cols[2], fld[2];
-    bool okc[2];
     lines[0] = threadIdx.x >> 4;
     lines[1] = lines[0] + 3 * CP;
 #pragma unroll
@@ -95,37 +96,40 @@ __device__ __forceinline__ void p3f_tile(const P3Args<float>& a, int col0, float
       const int l = lines[q];
       const int pair = l / 6, cc = (l / 3) & 1, t = l % 3;
       cols[q] = col0 + 2 * pair + cc;
-      okc[q] = cols[q] < a.ncols;
       fld[q] = 2 * t;
     }
     C2f2 v[24], w0[24];
 #pragma unroll
     for (int r = 0; r < 24; ++r) {
-      const int p = j + 16 * r;
       float2 z[2];
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
         float2 Xv = make_float2(0.f, 0.f), Yv = make_float2(0.f, 0.f);
-        const bool lo = p < H;
-        if (!(r >= 9 && r <= 15) && okc[q] && (lo || p > M - H)) {
-          const int k = lo ? p : M - p;
-          Xv = src(fld[q], cols[q], k);
-          Yv = src(fld[q] + 1, cols[q], k);
+        if (r <= 7 || (r == 8 && j == 0)) {
+          Xv = src(fld[q], cols[q], j + 16 * r);
+          Yv = src(fld[q] + 1, cols[q], j + 16 * r);
+        } else if (r >= 16) {
+          Xv = src(fld[q], cols[q], M - j - 16 * r);
+          Yv = src(fld[q] + 1, cols[q], M - j - 16 * r);
         }
         // Z = X + i Y with the Hermitian extension; the DC's imaginary parts
         // are dropped (the reference backend's c2r convention)
-        z[q] = p == 0 ? make_float2(Xv.x, Yv.x)
-             : lo ? make_float2(Xv.x - Yv.y, Xv.y + Yv.x) : make_float2(Xv.x + Yv.y, Yv.x - Xv.y);
+        if (r <= 8) {
+          z[q] = (r == 0 && j == 0) ? make_float2(Xv.x, Yv.x) : make_float2(Xv.x - Yv.y, Xv.y + Yv.x);
+        } else {
+          z[q] = make_float2(Xv.x + Yv.y, Yv.x - Xv.y);
+        }
       }
       v[r] = cpack(z[0], z[1]);
     }
     dft<f2, true, 24, false>(v, w0);
-    float2* la = X + lines[0] * G::LPA;
-    float2* lb = X + lines[1] * G::LPA;
+    // outputs at positions 24 j + r, index 25 j + r
+    float2* la = X + lines[0] * G::LPA + 25 * j;
+    float2* lb = X + lines[1] * G::LPA + 25 * j;
 #pragma unroll
     for (int r = 0; r < 24; ++r) {
-      la[G::ia(24 * j + r)] = clane0(v[r]);
-      lb[G::ia(24 * j + r)] = clane1(v[r]);
+      la[r] = clane0(v[r]);
+      lb[r] = clane1(v[r]);
     }
   }
   __syncthreads();
@@ -141,7 +145,7 @@ __device__ __forceinline__ void p3f_tile(const P3Args<float>& a, int col0, float
 #pragma unroll
     for (int t = 0; t < 3; ++t) {
 #pragma unroll
-      for (int r = 0; r < 16; ++r) z[t][r] = lines[t * G::LPA + G::ia(jp + 24 * r)];
+      for (int r = 0; r < 16; ++r) z[t][r] = lines[t * G::LPA + jp + 25 * r];   // position jp + 24 r
     }
     __syncthreads();   // XA is reused for the forward exchange below
     float2 w[16];
@@ -220,28 +224,26 @@ __device__ __forceinline__ void p3f_tile(const P3Args<float>& a, int col0, float
   __syncthreads();
 
   // ---- phase D: unpack the kept H modes of each real field and store --------
-  for (int e = threadIdx.x; e < CP * 3 * H; e += NT) {
-    const int k = e % H;
-    const int f = (e / H) % 3;
-    const int pr = e / (3 * H);
+#pragma unroll 1
+  for (int row = 0; row < CP * 3; ++row) {
+    const int pr = row / 3, f = row - 3 * pr;
     const float2* line = X + (3 * pr + f) * G::LPF;
-    const float2 zk = line[G::iff(k)];
-    const float2 zm = line[G::iff(k == 0 ? 0 : M - k)];
-    const float2 Xv = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-    const float2 Yv = make_float2(0.5f * (zk.y + zm.y), 0.5f * (zm.x - zk.x));
     const int ca = col0 + 2 * pr, cb = ca + 1;
-    if (f == 0) {
-      if (ca < a.ncols) {
-        a.out[(size_t)ca * H + k] = Xv;
-        a.out[a.fsout + (size_t)ca * H + k] = Yv;
-      }
-    } else if (f == 1) {
-      if (ca < a.ncols) a.out[2 * a.fsout + (size_t)ca * H + k] = Xv;
-      if (cb < a.ncols) a.out[2 * a.fsout + (size_t)cb * H + k] = Yv;
-    } else {
-      if (cb < a.ncols) {
-        a.out[(size_t)cb * H + k] = Xv;
-        a.out[a.fsout + (size_t)cb * H + k] = Yv;
+    float2* o0 = a.out + (size_t)(f == 0 ? ca : f == 1 ? ca : cb) * H;
+    for (int k = threadIdx.x; k < H; k += NT) {
+      const float2 zk = line[G::iff(k)];
+      const float2 zm = line[G::iff(k == 0 ? 0 : M - k)];
+      const float2 Xv = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+      const float2 Yv = make_float2(0.5f * (zk.y + zm.y), 0.5f * (zm.x - zk.x));
+      if (f == 0) {
+        o0[k] = Xv;                                     // c_x of column A
+        o0[a.fsout + k] = Yv;                           // c_y of column A
+      } else if (f == 1) {
+        o0[2 * a.fsout + k] = Xv;                       // c_z of column A
+        a.out[2 * a.fsout + (size_t)cb * H + k] = Yv;   // c_z of column B
+      } else {
+        o0[k] = Xv;                                     // c_x of column B
+        o0[a.fsout + k] = Yv;                           // c_y of column B
       }
     }
   }

@@ -171,6 +171,10 @@ struct vk_ctx {
     cudaGraphExec_t exec = nullptr;
     bool eager = false;
   } graphs[8];
+  // the ETD table of a new dt runs on a second stream beside the first
+  // stage's P1..P4 (only its P5 reads the table): fork at ev_dt, join at ev_etd
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_dt = nullptr, ev_etd = nullptr;
   bool use_graphs = true;
   bool has_state = false;
   bool umax_fresh = false;   // dsc->mx.umax2 describes the current state
@@ -260,7 +264,7 @@ vk::StageArgs<R> stage_args(vk_ctx* c, int op, void* out) {
 }
 
 template <typename R>
-cudaError_t nle_t(vk_ctx* c, const void* in, int op, void* out, int diag) {
+cudaError_t nle_t(vk_ctx* c, const void* in, int op, void* out, int diag, cudaEvent_t wait_p5) {
   vk::NleParams<R> p{};
   p.N = c->N;
   p.ks = c->ks;
@@ -272,12 +276,15 @@ cudaError_t nle_t(vk_ctx* c, const void* in, int op, void* out, int diag) {
   p.st = stage_args<R>(c, op, out);
   p.st.diag = diag;
   p.timer = c->prof;
+  p.wait_p5 = wait_p5;
   return vk::Engine<R>::nle(p, c->stream);
 }
 
-// diag: DiagBits to accumulate from the new state (final stages only).
-cudaError_t nle(vk_ctx* c, const void* in, int op, void* out = nullptr, int diag = 0) {
-  return c->fp32 ? nle_t<float>(c, in, op, out, diag) : nle_t<double>(c, in, op, out, diag);
+// diag: DiagBits to accumulate from the new state (final stages only);
+// wait_p5: an event that P5 (the stage epilogue) waits for.
+cudaError_t nle(vk_ctx* c, const void* in, int op, void* out = nullptr, int diag = 0,
+                cudaEvent_t wait_p5 = nullptr) {
+  return c->fp32 ? nle_t<float>(c, in, op, out, diag, wait_p5) : nle_t<double>(c, in, op, out, diag, wait_p5);
 }
 
 template <typename R>
@@ -321,6 +328,7 @@ cudaError_t etd_table(vk_ctx* c, int force) {
 cudaError_t enqueue_step(vk_ctx* c, int diag) {
   cudaError_t e;
   const bool rk4 = c->cfg.integrator == VK_INTEGRATOR_RK4;
+  cudaEvent_t etd_ready = nullptr;
   if (c->cfg.dt_mode == VK_DT_CFL) {
     if (!c->umax_fresh) {
       e = ngrid(c, 1);
@@ -331,9 +339,17 @@ cudaError_t enqueue_step(vk_ctx* c, int diag) {
       e = vk::launch_cfl_update(c->dsc, dx_of(c), c->cfg.nu, c->cfg.cfl_safety, 0, c->stream);
     }
     if (e != cudaSuccess) return e;
-    if (!rk4) {
-      e = etd_table(c, 0);
+    if (!rk4 && c->prof) {
+      e = etd_table(c, 0);   // in order, so that the pass timers see it alone
       if (e != cudaSuccess) return e;
+    } else if (!rk4) {
+      // the table for the new dt beside the first stage's P1..P4
+      if ((e = cudaEventRecord(c->ev_dt, c->stream)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(c->side, c->ev_dt, 0)) != cudaSuccess) return e;
+      e = vk::launch_etd_table(c->etd, c->n_etd, c->cfg.nu, c->ks * c->ks, c->dsc, 0, c->cc, c->side);
+      if (e != cudaSuccess) return e;
+      if ((e = cudaEventRecord(c->ev_etd, c->side)) != cudaSuccess) return e;
+      etd_ready = c->ev_etd;
     }
   }
   int ops[4];
@@ -345,7 +361,7 @@ cudaError_t enqueue_step(vk_ctx* c, int diag) {
     ops[0] = vk::ST_ETD_REF_1; ops[1] = vk::ST_ETD_REF_2; ops[2] = vk::ST_ETD_REF_3; ops[3] = vk::ST_ETD_4;
   }
   for (int s = 0; s < 4; ++s) {
-    e = nle(c, s == 0 ? c->u : c->temp, ops[s], nullptr, s == 3 ? diag : 0);
+    e = nle(c, s == 0 ? c->u : c->temp, ops[s], nullptr, s == 3 ? diag : 0, s == 0 ? etd_ready : nullptr);
     if (e != cudaSuccess) return e;
   }
   vk::TimerScope ts(c->prof, vk::PASS_SMALL, c->stream);
@@ -520,6 +536,9 @@ void free_ctx(vk_ctx* c) {
                   c->etd, c->dsc, c->records, c->part, c->dspec, c->dpart};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (c->ev_dt) cudaEventDestroy(c->ev_dt);
+  if (c->ev_etd) cudaEventDestroy(c->ev_etd);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -601,6 +620,9 @@ int vk_create(const vk_config* cfg, vk_ctx** out) {
   if ((e = cudaGetDeviceProperties(&prop, cfg->device)) != cudaSuccess) return bail(e, "cudaGetDeviceProperties");
   c->dev_sms = prop.multiProcessorCount;
   if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
+  if ((e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
+  if ((e = cudaEventCreateWithFlags(&c->ev_dt, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
+  if ((e = cudaEventCreateWithFlags(&c->ev_etd, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
   const size_t vbytes = 3 * c->cs * c->esz;
   if ((e = cudaMalloc(&c->u, vbytes)) != cudaSuccess) return bail(e, "cudaMalloc(u)");
   if ((e = cudaMalloc(&c->temp, vbytes)) != cudaSuccess) return bail(e, "cudaMalloc(temp)");

@@ -129,6 +129,10 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
   }
   // P5 (the DIAG instance when the stage also feeds fused diagnostics)
+  if (p.wait_p5) {
+    e = cudaStreamWaitEvent(s, p.wait_p5, 0);
+    if (e != cudaSuccess) return e;
+  }
   {
     TimerScope ts(p.timer, PASS_P5, s);
     constexpr int NL = P5Lines<R, M>::value;

@@ -109,6 +109,7 @@ template <typename R> struct NleParams {
   const C2<R>* twM;                    // twiddles, length M = 3N/2
   StageArgs<R> st;
   KTimer* timer;                       // null unless profiling
+  cudaEvent_t wait_p5;                 // if set, P5 waits for it (work P5 alone depends on)
 };
 
 template <typename R> struct NgridParams {

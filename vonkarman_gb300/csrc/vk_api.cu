@@ -277,6 +277,7 @@ cudaError_t nle_t(vk_ctx* c, const void* in, int op, void* out, int diag, cudaEv
   p.st.diag = diag;
   p.timer = c->prof;
   p.wait_p5 = wait_p5;
+  p.async_err = &c->dsc->async_timeout;
   return vk::Engine<R>::nle(p, c->stream);
 }
 
@@ -464,6 +465,7 @@ void fill_tier1(const vk_ctx* c, const vk::DevScalars& d, uint64_t step, vk_tier
 int read_scalars(vk_ctx* c, vk::DevScalars* h) {
   VK_CHECK(c, cudaMemcpyAsync(h, c->dsc, sizeof(vk::DevScalars), cudaMemcpyDeviceToHost, c->stream));
   VK_CHECK(c, cudaStreamSynchronize(c->stream));
+  if (h->async_timeout) return fail(c, VK_ERR_CUDA, "a bulk copy into shared memory did not arrive in time");
   if (h->nonfinite || h->mx.nan_flag)
     return fail(c, VK_ERR_NONFINITE, "non-finite value (NaN or Inf) in the solver state");
   return VK_OK;
@@ -971,6 +973,7 @@ cudaError_t nle_stage_t(vk_ctx* c, const void* in, int op, void* u, void* temp, 
   p.st.temp = (C2<R>*)temp;
   p.st.u_out = (C2<R>*)u_out;
   p.timer = c->prof;
+  p.async_err = &c->dsc->async_timeout;
   return vk::Engine<R>::nle(p, c->stream);
 }
 

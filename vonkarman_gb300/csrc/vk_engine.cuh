@@ -10,6 +10,13 @@
 #include "vk_adjoint.cuh"
 #include "vk_lines.cuh"
 #include "vk_p3f.cuh"
+#include "vk_tma.cuh"
+
+// P1 with its input tiles staged in shared memory by the tensor-memory
+// accelerator (k_lines_tma) instead of direct loads (k_lines)
+#ifndef VK_P1_TMA
+#define VK_P1_TMA 0
+#endif
 #include "vk_reduce.cuh"
 
 namespace vk {
@@ -69,6 +76,36 @@ inline cudaError_t launch_lines(const Op& op, int nouter, const C2<R>* tw, cudaS
 }
 
 
+// P1 through k_lines_tma: N x (N H) lines of 3 components at component
+// stride cs (complex values), NLINES lines per CTA.
+template <int L, int NLINES, class Op>
+inline cudaError_t launch_lines_tma(const Op& op, int nouter, const float2* tw, const float2* in, size_t cs,
+                                    int* err, cudaStream_t s) {
+  constexpr int NSRC = 2 * L / 3;
+  constexpr int NT = cmin(rthreads<float, L, NLINES>(), 384);
+  const int nlines = nouter * op.hz;
+  if (nlines % NLINES != 0 || (reinterpret_cast<uintptr_t>(in) & 15u) != 0 || ((cs * sizeof(float2)) & 15u) != 0)
+    return cudaErrorInvalidValue;
+  const TensorMapEncodeTiledFn enc = tensor_map_encoder();
+  if (!enc) return cudaErrorNotSupported;
+  CUtensorMap map;
+  const cuuint64_t dims[3] = {(cuuint64_t)2 * nlines, (cuuint64_t)NSRC, 3};
+  const cuuint64_t strides[2] = {(cuuint64_t)nlines * sizeof(float2), (cuuint64_t)cs * sizeof(float2)};
+  const cuuint32_t box[3] = {2 * NLINES, NSRC, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2*>(in), dims, strides, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  const size_t smem = (size_t)(NSRC * NLINES + rsmem_elems<float, L, NLINES>()) * sizeof(float2) + 128;
+  constexpr auto kern = k_lines_tma<L, NLINES, NT, Op>;
+  cudaError_t e = prepare_kernel<kern>(smem);
+  if (e != cudaSuccess) return e;
+  kern<<<op.nfields * (nlines / NLINES), NT, smem, s>>>(op, tw, map, err);
+  return cudaGetLastError();
+}
+
+
 template <typename R, int N>
 inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   constexpr int M = 3 * N / 2;
@@ -83,7 +120,12 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
   {
     TimerScope ts(p.timer, PASS_P1, s);
     OpXInv<R, N, M> o{5, H, N, M, (R)(1.0 / ((double)N * N * N)), ks, p.in, p.cs, p.bufA, fsA1};
-    e = launch_lines<R, M, true, true>(o, N, p.twM, s);
+#if VK_P1_TMA
+    if constexpr (sizeof(R) == 4 && M == 384 && (N * H) % 16 == 0)
+      e = launch_lines_tma<M, 16>(o, N, p.twM, p.in, p.cs, p.async_err, s);
+    else
+#endif
+      e = launch_lines<R, M, true, true>(o, N, p.twM, s);
     if (e != cudaSuccess) return e;
   }
   // P2

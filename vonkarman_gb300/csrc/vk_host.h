@@ -29,6 +29,7 @@ struct DevScalars {
   double cfl_dt;          // last CFL estimate
   int etd_recompute;      // set by the CFL update, read by the ETD table kernel
   int nonfinite;          // sticky: a NaN/Inf was seen in the state (CFL maxima or a step's output)
+  int async_timeout;      // sticky: a bulk copy into shared memory did not arrive in time
   MaxOut mx;              // N-grid maxima of the current state
   double sums[4];         // Tier-1 sums (energy, enstrophy, helicity, superhelicity), raw
 };
@@ -110,6 +111,7 @@ template <typename R> struct NleParams {
   StageArgs<R> st;
   KTimer* timer;                       // null unless profiling
   cudaEvent_t wait_p5;                 // if set, P5 waits for it (work P5 alone depends on)
+  int* async_err;                      // set by a kernel whose bulk copy timed out
 };
 
 template <typename R> struct NgridParams {

@@ -80,6 +80,7 @@ template <typename R, int GN = 0, int GM = 0> struct OpXInv {
   VK_GRID_DIMS(GN, GM)
   VK_PAD_ZEROS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : 1; }
+  __host__ __device__ __forceinline__ int src_component(int f) const { return f < 3 ? f : f - 2; }
   template <int K> __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
     const int ix = unpad_pos(p, n_(), m_());
     const int c = K == 0 ? f : f - 2;

@@ -36,6 +36,12 @@
 #include "vk_lines.cuh"
 #include "vk_pair.cuh"
 
+// phase D from the registers of phase C with a shuffle for the Hermitian
+// partner (1), or through shared memory after a barrier (0)
+#ifndef VK_P3F_UNPACK_REGS
+#define VK_P3F_UNPACK_REGS 1
+#endif
+
 namespace vk {
 
 template <int CP>
@@ -216,6 +222,35 @@ __device__ __forceinline__ void p3f_tile(const P3Args<float>& a, int col0, float
     for (int r = 0; r < 24; ++r) v[r] = line[G::iff(j + 16 * r)];
 #pragma unroll
     for (int r = 1; r < 24; ++r) w[r] = twf[(r - 1) * 16 + j];
+#if VK_P3F_UNPACK_REGS
+    dft<float, false, 24, true>(v, w);
+    // ---- phase D: unpack the kept modes k = j + 16 r <= 128 from registers.
+    // Z(M - k) is output 23 - r of lane 16 - j of this 16-lane group (the
+    // line's), or, for j = 0, output (24 - r) mod 24 of this lane.
+    const int lane = threadIdx.x & 31;
+    const int src = (lane & 16) | ((16 - j) & 15);
+    const int ca = col0 + 2 * pair, cb = ca + 1;
+    float2* o0 = a.out + (size_t)(f == 2 ? cb : ca) * H;
+#pragma unroll
+    for (int r = 0; r <= 8; ++r) {
+      const float2 zs = make_float2(__shfl_sync(0xffffffffu, v[23 - r].x, src),
+                                    __shfl_sync(0xffffffffu, v[23 - r].y, src));
+      const float2 zk = v[r];
+      const float2 zm = j == 0 ? v[(24 - r) % 24] : zs;
+      if (r == 8 && j != 0) continue;   // k = 128 only at j = 0
+      const int k = j + 16 * r;
+      const float2 Xv = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+      const float2 Yv = make_float2(0.5f * (zk.y + zm.y), 0.5f * (zm.x - zk.x));
+      if (f == 1) {
+        o0[2 * a.fsout + k] = Xv;                       // c_z of column A
+        a.out[2 * a.fsout + (size_t)cb * H + k] = Yv;   // c_z of column B
+      } else {
+        o0[k] = Xv;                                     // c_x of column A (f = 0) / B (f = 2)
+        o0[a.fsout + k] = Yv;                           // c_y
+      }
+    }
+  }
+#else
     __syncthreads();   // outputs go back into the same line positions' buffer
     dft<float, false, 24, true>(v, w);
 #pragma unroll
@@ -247,6 +282,7 @@ __device__ __forceinline__ void p3f_tile(const P3Args<float>& a, int col0, float
       }
     }
   }
+#endif
 }
 
 template <int CP>

@@ -17,6 +17,14 @@
 #ifndef VK_P1_TMA
 #define VK_P1_TMA 0
 #endif
+// L2 prefetch of the inputs one residency wave ahead in the x-inverse passes
+// (P1, NX: the op supplies prefetch_row) and in k_p3f
+#ifndef VK_LINES_PREFETCH
+#define VK_LINES_PREFETCH 1
+#endif
+#ifndef VK_P3F_PREFETCH
+#define VK_P3F_PREFETCH 1
+#endif
 #include "vk_reduce.cuh"
 
 namespace vk {
@@ -61,6 +69,15 @@ template <typename R, int L, bool XAXIS, class Op> struct NLof {
   static constexpr int value = (sizeof(R) == 4 && L <= LMAX) ? 16 : 8;
 };
 
+// Multiprocessors of the current device (the L2 prefetch distances are
+// resident CTAs per SM times this).
+inline int device_sms() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0;
+  return n;
+}
+
 template <typename R, int L, bool INV, bool XAXIS = false, class Op>
 inline cudaError_t launch_lines(const Op& op, int nouter, const C2<R>* tw, cudaStream_t s) {
   constexpr int NLINES = NLof<R, L, XAXIS, Op>::value;
@@ -71,7 +88,13 @@ inline cudaError_t launch_lines(const Op& op, int nouter, const C2<R>* tw, cudaS
   if (e != cudaSuccess) return e;
   const int nlines = nouter * op.hz;
   const int ntiles = (nlines + NLINES - 1) / NLINES;
-  kern<<<op.nfields * ntiles, NT, smem, s>>>(op, tw, nlines);
+  // L2 prefetch one residency wave ahead (the CTAs per SM of this instance)
+  int pf = 0;
+  if (VK_LINES_PREFETCH) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem) == cudaSuccess) pf = per_sm * device_sms();
+  }
+  kern<<<op.nfields * ntiles, NT, smem, s>>>(op, tw, nlines, pf);
   return cudaGetLastError();
 }
 
@@ -146,7 +169,13 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     constexpr auto kern = k_p3f<CP>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
-    kern<<<ntiles, P3F<CP>::NT, smem, s>>>(a, p.twM);
+    int pf = 0;
+    if (VK_P3F_PREFETCH) {
+      int per_sm = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, P3F<CP>::NT, smem) == cudaSuccess)
+        pf = per_sm * device_sms();
+    }
+    kern<<<ntiles, P3F<CP>::NT, smem, s>>>(a, p.twM, pf);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   } else {

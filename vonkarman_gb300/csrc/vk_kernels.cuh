@@ -27,6 +27,18 @@ namespace vk {
 // ---------------------------------------------------------------------------
 // Index helpers
 // ---------------------------------------------------------------------------
+// L2 prefetch hints for the inputs of a CTA that starts later (the one a
+// residency wave ahead), so that its first-stage loads hit L2 instead of
+// DRAM: one cache line, or a 16-byte-aligned range whose size is a multiple
+// of 16 bytes (bulk form).  Hints only: nothing is returned or waited for.
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+
 // padded position -> N-grid index, or -1 for a zero-padded slot
 // (inverse of dealiased.rs:129-131)
 __device__ __forceinline__ int unpad_pos(int p, int N, int M) {
@@ -81,6 +93,11 @@ template <typename R, int GN = 0, int GM = 0> struct OpXInv {
   VK_PAD_ZEROS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : 1; }
   __host__ __device__ __forceinline__ int src_component(int f) const { return f < 3 ? f : f - 2; }
+  // L2 prefetch of row t of the input tile of field f, lines [lam0, lam0 + nl)
+  // (the tile's rows are whole 128-byte lines)
+  __device__ __forceinline__ void prefetch_row(int f, int lam0, int, int t) const {
+    if (t < n_()) prefetch_l2(in + (size_t)src_component(f) * cs + (size_t)t * n_() * h_() + lam0);
+  }
   template <int K> __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
     const int ix = unpad_pos(p, n_(), m_());
     const int c = K == 0 ? f : f - 2;
@@ -179,6 +196,7 @@ template <typename R, int GN = 0, int GM = 0> struct OpYFwdTrunc {
   template <int K> __device__ __forceinline__ C2<R> load(int f, int x, int z, int p) const {
     return in[(size_t)f * fsin + ((x * m_() + p) * h_() + z)];
   }
+
   template <int K> __device__ __forceinline__ C2<R> prep(int, int, int, int, C2<R> v) const { return v; }
   __device__ __forceinline__ int out_index(int p) const { return unpad_pos(p, n_(), m_()); }
   __device__ __forceinline__ void store(int f, int x, int z, int i, C2<R> v) const {

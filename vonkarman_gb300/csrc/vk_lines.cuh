@@ -300,18 +300,37 @@ template <class Op> struct OpZeroRange<Op, std::void_t<decltype(Op::ZERO_LO)>> {
   static constexpr int lo = Op::ZERO_LO, hi = Op::ZERO_HI;
 };
 
+// Ops that supply prefetch_row(f, lam0, nl, t) (an L2 hint for row t of a
+// later CTA's input tile)
+template <class Op, class = void> struct OpHasPrefetch : std::false_type {};
+template <class Op>
+struct OpHasPrefetch<Op, std::void_t<decltype(std::declval<const Op&>().prefetch_row(0, 0, 0, 0))>> : std::true_type {};
+
 // Generic strided pass: NLINES consecutive lines lam = outer * hz + z of one
 // field per CTA (blockIdx.x = f + nfields * tile), so no z tile is partly
 // empty.  Op supplies kind(f) in [0, NKIND) (fields of one kind share their
 // load/prep code, which is specialised per kind), load<K>(f, outer, z, p)
 // (memory loads only, zero for padded positions), prep<K>(f, outer, z, p,
 // raw), out_index(p) (-1: dropped) and store(f, outer, z, i, v).  Lines past
-// the end (lam >= nlines) load line 0 and store nothing.
+// the end (lam >= nlines) load line 0 and store nothing.  pf: blocks ahead
+// whose input rows are prefetched into L2 (0 = none).
+
 template <typename R, int L, bool INV, int NLINES, int NT, class Op>
-__global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>()) k_lines(Op op, const C2<R>* __restrict__ tw, int nlines) {
+__global__ void __launch_bounds__(NT, lines_min_blocks<R, L, NT>())
+k_lines(Op op, const C2<R>* __restrict__ tw, int nlines, int pf) {
   static_assert(NT % NLINES == 0, "a thread keeps one line in every stage");
   extern __shared__ __align__(16) unsigned char vk_smem[];
   __shared__ C2<R> tw_s[twtab_elems<R, false>(L)];
+  // the input rows of the CTA pf blocks ahead (ops with prefetch_row, whole
+  // tiles whose rows are whole 128-byte lines)
+  if constexpr (OpHasPrefetch<Op>::value && NLINES * sizeof(C2<R>) == 128) {
+    const int b = (int)blockIdx.x + pf;
+    if (pf > 0 && b < (int)gridDim.x) {
+      const int lam0 = (b / op.nfields) * NLINES;
+      if (lam0 + NLINES <= nlines)
+        for (int t = threadIdx.x; t < L; t += NT) op.prefetch_row(b % op.nfields, lam0, NLINES, t);
+    }
+  }
   load_twtab<R, L, false, NT>(tw_s, tw);
   C2<R>* xb = reinterpret_cast<C2<R>*>(vk_smem);
   const int f = blockIdx.x % op.nfields;

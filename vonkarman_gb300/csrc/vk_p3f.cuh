@@ -300,10 +300,15 @@ __device__ __forceinline__ void p3f_twiddles(float2* twi, float2* twf, const flo
 // One tile per CTA, inputs straight from global memory.
 template <int CP>
 __global__ void __launch_bounds__(P3F<CP>::NT, 384 / P3F<CP>::NT)
-k_p3f(P3Args<float> a, const float2* __restrict__ tw) {
+k_p3f(P3Args<float> a, const float2* __restrict__ tw, int pf) {
   extern __shared__ __align__(16) unsigned char vk_smem[];
   __shared__ float2 twi[P3F_TWI];
   __shared__ float2 twf[P3F_TWF];
+  // L2 prefetch of the six input ranges of the CTA pf blocks ahead: per field
+  // its 2 CP consecutive columns, 2 CP x 129 complex values (16-byte multiples)
+  if (pf > 0 && threadIdx.x < 6 && blockIdx.x + pf < gridDim.x)
+    prefetch_l2_bulk(a.in + (size_t)threadIdx.x * a.fsin + (size_t)(blockIdx.x + pf) * (2 * CP * 129),
+                     2 * CP * 129 * sizeof(float2));
   p3f_twiddles<CP>(twi, twf, tw);
   float2* X = reinterpret_cast<float2*>(vk_smem);
   // the first barrier of the tile orders the twiddle loads before their use

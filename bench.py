@@ -204,7 +204,7 @@ def step_bytes(n: int, elem: int) -> float:
 # FP32-bulk at N=256, scaled to grid n by the padded columns x modes (M^2 H).
 NCU_TRAFFIC = {
     ("P3_z_c2r_cross_r2c", "fp64"): (128, 230142720 + 85930752),
-    ("P3_z_c2r_cross_r2c", "fp32bulk"): (256, 913160192 + 426381056),
+    ("P3_z_c2r_cross_r2c", "fp32bulk"): (256, 913113600 + 424164352),
 }
 
 
@@ -650,7 +650,8 @@ def run_ours(args, d: Dist):
                      "note": ("HBM fraction of the FP64 form's dominant kernel, which is bound by the FP64 pipe "
                               "(86 % of its cycles active in ncu): see fp64_roofline")
                      if args.precision == "fp64" else
-                     ("FP32-bulk P3: bound by the L1/shared-memory pipe (82 % in ncu at N=256)"
+                     ("FP32-bulk P3 (k_p3f): issue- and latency-bound in ncu at N=256 (53 % of issue slots, "
+                      "global-load latency the top stall, 4 CTAs of 96 threads per SM)"
                       if dom == "P3_z_c2r_cross_r2c" else None)},
         "fp64_roofline": {"kernel": dom, "achieved": dom_gflops, "peak": fp64_peak, "unit": "GFLOP/s",
                           "frac": dom_gflops / fp64_peak, "peak_source": "measured live (FP64 FMA probe)",

@@ -18,7 +18,7 @@
 #define VK_P1_TMA 0
 #endif
 // L2 prefetch of the inputs one residency wave ahead in the x-inverse passes
-// (P1, NX: the op supplies prefetch_row) and in k_p3f
+// (P1, NX: the op supplies prefetch_row) and in the FP32 z passes (k_p3f, k_p3)
 #ifndef VK_LINES_PREFETCH
 #define VK_LINES_PREFETCH 1
 #endif
@@ -188,7 +188,13 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     P3Args<R> a{M * M, p.bufB, fsB2, p.bufA, fsA3};
     const int nb = (M * M + 2 * CP - 1) / (2 * CP);
-    kern<<<nb, NT, smem, s>>>(a, p.twM);
+    int pf = 0;
+    if (sizeof(R) == 4 && VK_P3F_PREFETCH) {
+      int per_sm = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem) == cudaSuccess)
+        pf = per_sm * device_sms();
+    }
+    kern<<<nb, NT, smem, s>>>(a, p.twM, pf);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

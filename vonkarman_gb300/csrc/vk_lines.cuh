@@ -545,7 +545,7 @@ __host__ __device__ constexpr int p3_smem_lines() { return (p3_inplace<CP>() ? 6
 template <typename R, int M, int CP, int NT>
 __global__ void __launch_bounds__(NT, M >= 768 ? (sizeof(R) == 4 && p3_inplace<CP>() ? 3 : 1)
                                               : cmax(1, (sizeof(R) == 8 ? 768 : 512) / NT))
-k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
+k_p3(P3Args<R> a, const C2<R>* __restrict__ tw, int pf) {
   constexpr int N = 2 * M / 3;
   constexpr int H = N / 2 + 1;
   constexpr int LP = zpad_len<R>(M);
@@ -553,6 +553,14 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw) {
   constexpr bool INPL = p3_inplace<CP>();
   extern __shared__ __align__(16) unsigned char vk_smem[];
   __shared__ C2<R> tw_s[twtab_elems<R, true>(M)];
+  // L2 prefetch of the six input ranges of the CTA pf blocks ahead (FP32:
+  // 2 CP columns of H complex values per field, a multiple of 16 bytes at a
+  // 16-byte boundary)
+  if constexpr (sizeof(R) == 4) {
+    const int b = (int)blockIdx.x + pf;
+    if (pf > 0 && threadIdx.x < 6 && b < (int)gridDim.x && (b + 1) * 2 * CP <= a.ncols)
+      prefetch_l2_bulk(a.in + (size_t)threadIdx.x * a.fsin + (size_t)b * (2 * CP * H), 2 * CP * H * sizeof(C2<R>));
+  }
   load_twtab<R, M, true, NT>(tw_s, tw);
   C2<R>* A = reinterpret_cast<C2<R>*>(vk_smem);
   C2<R>* B = INPL ? A : A + NI * LP;

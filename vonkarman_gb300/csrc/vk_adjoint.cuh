@@ -78,6 +78,12 @@ template <typename R, int GN = 0, int GM = 0> struct OpAdjXInv {
   VK_GRID_DIMS(GN, GM)
   VK_PAD_ZEROS(GN, GM)
   __host__ __device__ __forceinline__ int kind(int f) const { return f < 3 ? 0 : f < 5 ? 1 : 2; }
+  // L2 prefetch of row t of the input tile of field f (as OpXInv's)
+  __device__ __forceinline__ void prefetch_row(int f, int lam0, int, int t) const {
+    const C2<R>* src = f < 5 ? in : cb;
+    const int c = f < 3 ? f : f < 5 ? f - 2 : f - 5;
+    if (t < n_()) prefetch_l2(src + (size_t)c * cs + (size_t)t * n_() * h_() + lam0);
+  }
   template <int K> __device__ __forceinline__ C2<R> load(int f, int iy, int z, int p) const {
     const int ix = unpad_pos(p, n_(), m_());
     const C2<R>* src = K == 2 ? cb : in;
@@ -165,13 +171,21 @@ __host__ __device__ constexpr int adj_z_smem_elems() {
 // (ab_z + i ob_x), (ob_y + i ob_z) of column c.
 template <typename R, int M, int CP, int NT>
 __global__ void __launch_bounds__(NT, M >= 768 ? 1 : cmax(1, (sizeof(R) == 8 ? 768 : 512) / NT))
-k_adj_z(A3Args<R> a, const C2<R>* __restrict__ tw) {
+k_adj_z(A3Args<R> a, const C2<R>* __restrict__ tw, int pf) {
   constexpr int N = 2 * M / 3;
   constexpr int H = N / 2 + 1;
   constexpr int LP = zpad_len<R>(M);
   constexpr int NI = 9 * CP, NF = 6 * CP;
   extern __shared__ __align__(16) unsigned char vk_smem[];
   __shared__ C2<R> tw_s[twtab_elems<R, true>(M)];
+  // L2 prefetch of the nine input ranges of the CTA pf blocks ahead (FP32:
+  // per field 2 CP columns of H complex values, a multiple of 16 bytes at a
+  // 16-byte boundary)
+  if constexpr (sizeof(R) == 4) {
+    const int b = (int)blockIdx.x + pf;
+    if (pf > 0 && threadIdx.x < 9 && b < (int)gridDim.x && (b + 1) * 2 * CP <= a.ncols)
+      prefetch_l2_bulk(a.in + (size_t)threadIdx.x * a.fsin + (size_t)b * (2 * CP * H), 2 * CP * H * sizeof(C2<R>));
+  }
   load_twtab<R, M, true, NT>(tw_s, tw);
   C2<R>* A = reinterpret_cast<C2<R>*>(vk_smem);   // NI lines
   C2<R>* B = A + NI * LP;                          // NF lines

@@ -18,7 +18,8 @@
 #define VK_P1_TMA 0
 #endif
 // L2 prefetch of the inputs one residency wave ahead in the x-inverse passes
-// (P1, NX: the op supplies prefetch_row) and in the FP32 z passes (k_p3f, k_p3)
+// (P1, NX: the op supplies prefetch_row) and in the FP32 z passes (k_p3f,
+// k_p3, k_nz_max)
 #ifndef VK_LINES_PREFETCH
 #define VK_LINES_PREFETCH 1
 #endif
@@ -76,6 +77,16 @@ inline int device_sms() {
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return 0;
   return n;
+}
+
+// L2 prefetch distance of the FP32 column-pair z passes (k_p3, k_nz_max):
+// one residency wave (0 = off, and for FP64, whose passes the FP64 pipe bounds)
+template <typename R, class K>
+inline int zpass_prefetch_distance(K kern, int nt, size_t smem) {
+  int per_sm = 0;
+  if (sizeof(R) != 4 || !VK_P3F_PREFETCH || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem) != cudaSuccess)
+    return 0;
+  return per_sm * device_sms();
 }
 
 template <typename R, int L, bool INV, bool XAXIS = false, class Op>
@@ -188,13 +199,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     P3Args<R> a{M * M, p.bufB, fsB2, p.bufA, fsA3};
     const int nb = (M * M + 2 * CP - 1) / (2 * CP);
-    int pf = 0;
-    if (sizeof(R) == 4 && VK_P3F_PREFETCH) {
-      int per_sm = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem) == cudaSuccess)
-        pf = per_sm * device_sms();
-    }
-    kern<<<nb, NT, smem, s>>>(a, p.twM, pf);
+    kern<<<nb, NT, smem, s>>>(a, p.twM, zpass_prefetch_distance<R>(kern, NT, smem));
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -276,7 +281,7 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     A3Args<R> a{M * M, p.bufB, fsB2, p.bufA, fsA3};
     const int nb = (M * M + 2 * CP - 1) / (2 * CP);
-    kern<<<nb, NT, smem, s>>>(a, p.twM);
+    kern<<<nb, NT, smem, s>>>(a, p.twM, zpass_prefetch_distance<R>(kern, NT, smem));
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -336,14 +341,14 @@ inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
     constexpr auto kern = k_nz_max<R, N, CP, true, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
-    kern<<<nb, NT, smem, s>>>(a, p.twN);
+    kern<<<nb, NT, smem, s>>>(a, p.twN, zpass_prefetch_distance<R>(kern, NT, smem));
   } else {
     constexpr int NT = nz_threads<R, N, CP, false>();
     const size_t smem = (size_t)3 * CP * zpad_len<R>(N) * sizeof(C2<R>);
     constexpr auto kern = k_nz_max<R, N, CP, false, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
-    kern<<<nb, NT, smem, s>>>(a, p.twN);
+    kern<<<nb, NT, smem, s>>>(a, p.twN, zpass_prefetch_distance<R>(kern, NT, smem));
   }
   return cudaGetLastError();
 }

@@ -649,7 +649,7 @@ __host__ __device__ constexpr int nz_threads() {
 
 template <typename R, int N, int CP, bool BOTH, int NT>
 __global__ void __launch_bounds__(NT, N >= 512 ? 1 : cmax(1, (sizeof(R) == 8 ? 768 : 512) / NT))
-k_nz_max(NZArgs<R> a, const C2<R>* __restrict__ tw) {
+k_nz_max(NZArgs<R> a, const C2<R>* __restrict__ tw, int pf) {
   constexpr int H = N / 2 + 1;
   constexpr int LPP = BOTH ? 6 : 3;   // lines per column pair
   constexpr int NL = LPP * CP;
@@ -659,6 +659,14 @@ k_nz_max(NZArgs<R> a, const C2<R>* __restrict__ tw) {
   __shared__ C2<R> tw_s[twtab_elems<R, true>(N)];
   __shared__ double red[2][32];
   __shared__ int redn;
+  // L2 prefetch of the input ranges of the CTA pf blocks ahead (FP32: per
+  // field 2 CP columns of H complex values, a multiple of 16 bytes at a
+  // 16-byte boundary)
+  if constexpr (sizeof(R) == 4) {
+    const int b = (int)blockIdx.x + pf;
+    if (pf > 0 && threadIdx.x < (BOTH ? 6 : 3) && b < (int)gridDim.x && (b + 1) * 2 * CP <= a.ncols)
+      prefetch_l2_bulk(a.in + (size_t)threadIdx.x * a.fs + (size_t)b * (2 * CP * H), 2 * CP * H * sizeof(C2<R>));
+  }
   load_twtab<R, N, true, NT>(tw_s, tw);
   if (threadIdx.x == 0) redn = 0;
   const int col0 = blockIdx.x * 2 * CP;

@@ -24,6 +24,12 @@
 #include "vk_kernels.cuh"
 #include "vk_reduce.cuh"
 
+// k_p3 (FP32) unpacks the forward's kept modes from the last stage's
+// registers (1) or through shared memory after a barrier (0)
+#ifndef VK_P3_ROW_UNPACK
+#define VK_P3_ROW_UNPACK 1
+#endif
+
 namespace vk {
 
 // FP32 plans: at most two stages up to L = 768, composite in-register radices
@@ -155,6 +161,12 @@ __host__ __device__ constexpr unsigned zero_mask(int nb, int rad, int z0, int z1
   return m;
 }
 
+// Store functors with a row<RAD, NS>(l, j, v) member take the last stage's
+// whole butterfly (outputs at positions j + NS r, r < RAD) in one call, so
+// that they can combine outputs across lanes (contiguous lines only).
+template <class ST, class = void> struct StoreTakesRows : std::false_type {};
+template <class ST> struct StoreTakesRows<ST, std::void_t<decltype(ST::kRowStore)>> : std::true_type {};
+
 template <typename R, int L, bool INV, int NT, int NLINES, class MAP, int S, int NS, bool SL = false, bool TT = false,
           int Z0 = 0, int Z1 = 0>
 struct RegStage {
@@ -241,7 +253,12 @@ struct RegStage {
         }
         dft<R, INV, RAD, (S > 0), S == 0 ? zero_mask(NB, RAD, Z0, Z1) : 0u>(v[q], w);
         const int base = (j - k) * RAD + k;
-        if constexpr (LAST) {
+        if constexpr (LAST && StoreTakesRows<ST>::value) {
+          // the whole butterfly (outputs j + NS r, j = base < NS) at once
+          static_assert(MAP::CONTIG && G % 32 == 0 && NT % 32 == 0 && NB == NS && (NS == 16 || NS == 32),
+                        "row stores: whole warps, butterfly j on lane j of an NS-lane group");
+          st.template row<RAD, NS>(l, base, v[q]);
+        } else if constexpr (LAST) {
 #pragma unroll
           for (int r = 0; r < RAD; ++r) st(l, base + r * NS, v[q][r]);
         } else {
@@ -542,6 +559,61 @@ template <int CP> __host__ __device__ constexpr bool p3_inplace() { return VK_P3
 template <typename R, int M, int CP>
 __host__ __device__ constexpr int p3_smem_lines() { return (p3_inplace<CP>() ? 6 : 12) * CP; }
 
+// Row unpack of the forward z transform of k_p3: butterfly j of forward line
+// l = t CP + pr holds Z(k) at k = j + NS r; the unpack of mode k needs
+// Z(M - k), which is output RAD - 1 - r of lane NS - j of the same NS-lane
+// group, or, for j = 0, output (RAD - r) mod RAD of this lane.  The kept
+// modes k < H are stored straight to global memory (the layout of k_p3's
+// shared-memory unpack below).
+template <typename R, int M, int CP>
+struct P3RowUnpack {
+  static constexpr bool kRowStore = true;
+  C2<R>* out; size_t fsout; int ncols; int col0;
+  template <int RAD, int NS>
+  __device__ __forceinline__ void row(int l, int j, const C2<R>* v) const {
+    constexpr int H = M / 3 + 1;
+    const int lane = threadIdx.x & 31;
+    const int src = (lane & ~(NS - 1)) | ((NS - j) & (NS - 1));
+    const int t = l / CP, pr = l - t * CP;
+    const int ca = col0 + 2 * pr, cb = ca + 1;
+#pragma unroll
+    for (int r = 0; r * NS < H; ++r) {
+      const C2<R> zs = cmk<R>(__shfl_sync(0xffffffffu, v[RAD - 1 - r].x, src),
+                              __shfl_sync(0xffffffffu, v[RAD - 1 - r].y, src));
+      const C2<R> z = v[r];
+      const C2<R> w = j == 0 ? v[(RAD - r) % RAD] : zs;
+      const int k = j + NS * r;
+      if (k >= H) continue;
+      const C2<R> X = cmk<R>(R(0.5) * (z.x + w.x), R(0.5) * (z.y - w.y));
+      const C2<R> Y = cmk<R>(R(0.5) * (z.y + w.y), R(0.5) * (w.x - z.x));
+      if (t == 0) {
+        if (ca < ncols) {
+          out[(size_t)ca * H + k] = X;
+          out[fsout + (size_t)ca * H + k] = Y;
+        }
+      } else if (t == 1) {
+        if (ca < ncols) out[2 * fsout + (size_t)ca * H + k] = X;
+        if (cb < ncols) out[2 * fsout + (size_t)cb * H + k] = Y;
+      } else {
+        if (cb < ncols) {
+          out[(size_t)cb * H + k] = X;
+          out[fsout + (size_t)cb * H + k] = Y;
+        }
+      }
+    }
+  }
+};
+// k_p3 unpacks from registers where the forward's last stage allows it: FP32
+// plans whose last stage has 16 or 32 butterflies per line over whole warps
+template <typename R, int M, int CP, int NT>
+__host__ __device__ constexpr bool p3_row_unpack() {
+  if (sizeof(R) != 4 || VK_P3_ROW_UNPACK == 0) return false;
+  constexpr int S = rstages<R, true>(M);
+  constexpr int RAD = rradix<R, true>(M, S - 1);
+  constexpr int NB = M / RAD;
+  return (NB == 16 || NB == 32) && (NB * 3 * CP) % 32 == 0 && NT % 32 == 0;
+}
+
 template <typename R, int M, int CP, int NT>
 __global__ void __launch_bounds__(NT, M >= 768 ? (sizeof(R) == 4 && p3_inplace<CP>() ? 3 : 1)
                                               : cmax(1, (sizeof(R) == 8 ? 768 : 512) / NT))
@@ -606,6 +678,13 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw, int pf) {
     A[(2 * CP + pr) * LP + zp] = cmk<R>(c[1][0], c[1][1]);
   }
   __syncthreads();
+  if constexpr (p3_row_unpack<R, M, CP, NT>()) {
+    // the kept modes unpacked from the last stage's registers
+    fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>, false, true>(
+        XF, tw_s, [&](int l, int p) { return A[l * LP + zi<R>(p)]; }, PrepNone{},
+        P3RowUnpack<R, M, CP>{a.out, a.fsout, a.ncols, col0});
+    return;
+  }
   fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>, false, true>(
       XF, tw_s, [&](int l, int p) { return A[l * LP + zi<R>(p)]; }, PrepNone{},
       [&](int l, int p, C2<R> v) { A[l * LP + zi<R>(p)] = v; });

@@ -165,6 +165,25 @@ __host__ __device__ constexpr int adj_z_smem_elems() {
   return 15 * CP * zpad_len<R>(M);
 }
 
+// Row unpack of A3's forward lines l = t 2CP + c: fields 2t and 2t + 1 of
+// column col0 + c (the layout of the shared-memory unpack in k_adj_z).
+template <typename R, int M, int CP>
+struct AdjZRowUnpack {
+  static constexpr bool kRowStore = true;
+  C2<R>* out; size_t fsout; int ncols; int col0;
+  template <int RAD, int NS>
+  __device__ __forceinline__ void row(int l, int j, const C2<R>* v) const {
+    constexpr int H = M / 3 + 1;
+    const int t = l / (2 * CP), col = col0 + (l - t * 2 * CP);
+    unpack_rows<R, RAD, NS, H>(j, v, [&](int k, const C2<R>& X, const C2<R>& Y) {
+      if (col < ncols) {
+        out[(size_t)(2 * t) * fsout + (size_t)col * H + k] = X;
+        out[(size_t)(2 * t + 1) * fsout + (size_t)col * H + k] = Y;
+      }
+    });
+  }
+};
+
 // On the register engine: inverse lines l < 8 CP are the packed pair
 // t = l / 2CP of column c = l % 2CP; lines 8 CP + pr carry c_bar_z of the two
 // columns of pair pr.  Forward lines l = t * 2CP + c: (ab_x + i ab_y),
@@ -239,6 +258,13 @@ k_adj_z(A3Args<R> a, const C2<R>* __restrict__ tw, int pf) {
     }
   }
   __syncthreads();
+  if constexpr (z_row_unpack<R, M, NF, NT>()) {
+    // the kept modes unpacked from the last stage's registers
+    fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>, false, true>(
+        A, tw_s, [&](int l, int p) { return B[l * LP + zi<R>(p)]; }, PrepNone{},
+        AdjZRowUnpack<R, M, CP>{a.out, a.fsout, a.ncols, col0});
+    return;
+  }
   fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>, false, true>(
       A, tw_s, [&](int l, int p) { return B[l * LP + zi<R>(p)]; }, PrepNone{},
       [&](int l, int p, C2<R> v) { B[l * LP + zi<R>(p)] = v; });

@@ -559,12 +559,31 @@ template <int CP> __host__ __device__ constexpr bool p3_inplace() { return VK_P3
 template <typename R, int M, int CP>
 __host__ __device__ constexpr int p3_smem_lines() { return (p3_inplace<CP>() ? 6 : 12) * CP; }
 
-// Row unpack of the forward z transform of k_p3: butterfly j of forward line
-// l = t CP + pr holds Z(k) at k = j + NS r; the unpack of mode k needs
-// Z(M - k), which is output RAD - 1 - r of lane NS - j of the same NS-lane
-// group, or, for j = 0, output (RAD - r) mod RAD of this lane.  The kept
-// modes k < H are stored straight to global memory (the layout of k_p3's
-// shared-memory unpack below).
+// Hermitian unpack of a forward line from the last stage's registers:
+// butterfly j (lane j of an NS-lane group) holds Z(k) at k = j + NS r, r <
+// RAD; the unpack of mode k needs Z(L - k), which is output RAD - 1 - r of
+// lane NS - j of the same group, or, for j = 0, output (RAD - r) mod RAD of
+// this lane.  f(k, X, Y) receives the two real fields' modes k < H.  All
+// lanes of the warp must call it.
+template <typename R, int RAD, int NS, int H, class F>
+__device__ __forceinline__ void unpack_rows(int j, const C2<R>* v, const F& f) {
+  const int lane = threadIdx.x & 31;
+  const int src = (lane & ~(NS - 1)) | ((NS - j) & (NS - 1));
+#pragma unroll
+  for (int r = 0; r * NS < H; ++r) {
+    const C2<R> zs = cmk<R>(__shfl_sync(0xffffffffu, v[RAD - 1 - r].x, src),
+                            __shfl_sync(0xffffffffu, v[RAD - 1 - r].y, src));
+    const C2<R> z = v[r];
+    const C2<R> w = j == 0 ? v[(RAD - r) % RAD] : zs;
+    const int k = j + NS * r;
+    if (k >= H) continue;
+    f(k, cmk<R>(R(0.5) * (z.x + w.x), R(0.5) * (z.y - w.y)), cmk<R>(R(0.5) * (z.y + w.y), R(0.5) * (w.x - z.x)));
+  }
+}
+
+// Row unpack of the forward z transform of k_p3 (forward line l = t CP + pr):
+// the kept modes go straight to global memory, in the layout of k_p3's
+// shared-memory unpack below.
 template <typename R, int M, int CP>
 struct P3RowUnpack {
   static constexpr bool kRowStore = true;
@@ -572,20 +591,9 @@ struct P3RowUnpack {
   template <int RAD, int NS>
   __device__ __forceinline__ void row(int l, int j, const C2<R>* v) const {
     constexpr int H = M / 3 + 1;
-    const int lane = threadIdx.x & 31;
-    const int src = (lane & ~(NS - 1)) | ((NS - j) & (NS - 1));
     const int t = l / CP, pr = l - t * CP;
     const int ca = col0 + 2 * pr, cb = ca + 1;
-#pragma unroll
-    for (int r = 0; r * NS < H; ++r) {
-      const C2<R> zs = cmk<R>(__shfl_sync(0xffffffffu, v[RAD - 1 - r].x, src),
-                              __shfl_sync(0xffffffffu, v[RAD - 1 - r].y, src));
-      const C2<R> z = v[r];
-      const C2<R> w = j == 0 ? v[(RAD - r) % RAD] : zs;
-      const int k = j + NS * r;
-      if (k >= H) continue;
-      const C2<R> X = cmk<R>(R(0.5) * (z.x + w.x), R(0.5) * (z.y - w.y));
-      const C2<R> Y = cmk<R>(R(0.5) * (z.y + w.y), R(0.5) * (w.x - z.x));
+    unpack_rows<R, RAD, NS, H>(j, v, [&](int k, const C2<R>& X, const C2<R>& Y) {
       if (t == 0) {
         if (ca < ncols) {
           out[(size_t)ca * H + k] = X;
@@ -600,18 +608,19 @@ struct P3RowUnpack {
           out[fsout + (size_t)cb * H + k] = Y;
         }
       }
-    }
+    });
   }
 };
-// k_p3 unpacks from registers where the forward's last stage allows it: FP32
-// plans whose last stage has 16 or 32 butterflies per line over whole warps
-template <typename R, int M, int CP, int NT>
-__host__ __device__ constexpr bool p3_row_unpack() {
+// Forward z transforms of NF lines unpack from registers where the last
+// stage allows it: FP32 plans whose last stage has 16 or 32 butterflies per
+// line over whole warps
+template <typename R, int M, int NF, int NT>
+__host__ __device__ constexpr bool z_row_unpack() {
   if (sizeof(R) != 4 || VK_P3_ROW_UNPACK == 0) return false;
   constexpr int S = rstages<R, true>(M);
   constexpr int RAD = rradix<R, true>(M, S - 1);
   constexpr int NB = M / RAD;
-  return (NB == 16 || NB == 32) && (NB * 3 * CP) % 32 == 0 && NT % 32 == 0;
+  return (NB == 16 || NB == 32) && (NB * NF) % 32 == 0 && NT % 32 == 0;
 }
 
 template <typename R, int M, int CP, int NT>
@@ -678,7 +687,7 @@ k_p3(P3Args<R> a, const C2<R>* __restrict__ tw, int pf) {
     A[(2 * CP + pr) * LP + zp] = cmk<R>(c[1][0], c[1][1]);
   }
   __syncthreads();
-  if constexpr (p3_row_unpack<R, M, CP, NT>()) {
+  if constexpr (z_row_unpack<R, M, NF, NT>()) {
     // the kept modes unpacked from the last stage's registers
     fft_lines<R, M, false, NT, NF, MapContig<R, M, NF>, false, true>(
         XF, tw_s, [&](int l, int p) { return A[l * LP + zi<R>(p)]; }, PrepNone{},

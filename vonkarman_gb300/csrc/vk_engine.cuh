@@ -70,23 +70,34 @@ template <typename R, int L, bool XAXIS, class Op> struct NLof {
   static constexpr int value = (sizeof(R) == 4 && L <= LMAX) ? 16 : 8;
 };
 
-// Multiprocessors of the current device (the L2 prefetch distances are
-// resident CTAs per SM times this).
-inline int device_sms() {
-  int dev = 0, n = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+// One residency wave of kernel instance KERN on the current device (resident
+// CTAs per SM at nt threads and smem bytes, times the SMs): the L2 prefetch
+// distance of the passes that hint a later CTA's inputs.  Cached per device,
+// as prepare_kernel's opt-in is (0 when a query fails).
+template <auto KERN>
+inline int wave_blocks(int nt, size_t smem) {
+  static std::atomic<int> cache[64];   // wave + 1 once known
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (dev < 64) {
+    const int v = cache[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v - 1;
+  }
+  int per_sm = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, KERN, nt, smem) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return 0;
-  return n;
+  const int w = per_sm * sms;
+  if (dev < 64) cache[dev].store(w + 1, std::memory_order_relaxed);
+  return w;
 }
 
-// L2 prefetch distance of the FP32 column-pair z passes (k_p3, k_nz_max):
-// one residency wave (0 = off, and for FP64, whose passes the FP64 pipe bounds)
-template <typename R, class K>
-inline int zpass_prefetch_distance(K kern, int nt, size_t smem) {
-  int per_sm = 0;
-  if (sizeof(R) != 4 || !VK_P3F_PREFETCH || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem) != cudaSuccess)
-    return 0;
-  return per_sm * device_sms();
+// L2 prefetch distance of the FP32 column-pair z passes (k_p3, k_nz_max,
+// k_adj_z): one residency wave (0 = off, and for FP64, whose passes the FP64
+// pipe bounds)
+template <typename R, auto KERN>
+inline int zpass_prefetch_distance(int nt, size_t smem) {
+  return sizeof(R) == 4 && VK_P3F_PREFETCH ? wave_blocks<KERN>(nt, smem) : 0;
 }
 
 template <typename R, int L, bool INV, bool XAXIS = false, class Op>
@@ -99,12 +110,8 @@ inline cudaError_t launch_lines(const Op& op, int nouter, const C2<R>* tw, cudaS
   if (e != cudaSuccess) return e;
   const int nlines = nouter * op.hz;
   const int ntiles = (nlines + NLINES - 1) / NLINES;
-  // L2 prefetch one residency wave ahead (the CTAs per SM of this instance)
-  int pf = 0;
-  if (VK_LINES_PREFETCH) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem) == cudaSuccess) pf = per_sm * device_sms();
-  }
+  // L2 prefetch one residency wave ahead
+  const int pf = VK_LINES_PREFETCH ? wave_blocks<kern>(NT, smem) : 0;
   kern<<<op.nfields * ntiles, NT, smem, s>>>(op, tw, nlines, pf);
   return cudaGetLastError();
 }
@@ -180,12 +187,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     constexpr auto kern = k_p3f<CP>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
-    int pf = 0;
-    if (VK_P3F_PREFETCH) {
-      int per_sm = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, P3F<CP>::NT, smem) == cudaSuccess)
-        pf = per_sm * device_sms();
-    }
+    const int pf = VK_P3F_PREFETCH ? wave_blocks<kern>(P3F<CP>::NT, smem) : 0;
     kern<<<ntiles, P3F<CP>::NT, smem, s>>>(a, p.twM, pf);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -199,7 +201,7 @@ inline cudaError_t nle_n(const NleParams<R>& p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     P3Args<R> a{M * M, p.bufB, fsB2, p.bufA, fsA3};
     const int nb = (M * M + 2 * CP - 1) / (2 * CP);
-    kern<<<nb, NT, smem, s>>>(a, p.twM, zpass_prefetch_distance<R>(kern, NT, smem));
+    kern<<<nb, NT, smem, s>>>(a, p.twM, zpass_prefetch_distance<R, kern>(NT, smem));
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -281,7 +283,7 @@ inline cudaError_t nla_n(const NlaParams<R>& p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     A3Args<R> a{M * M, p.bufB, fsB2, p.bufA, fsA3};
     const int nb = (M * M + 2 * CP - 1) / (2 * CP);
-    kern<<<nb, NT, smem, s>>>(a, p.twM, zpass_prefetch_distance<R>(kern, NT, smem));
+    kern<<<nb, NT, smem, s>>>(a, p.twM, zpass_prefetch_distance<R, kern>(NT, smem));
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -341,14 +343,14 @@ inline cudaError_t ngrid_n(const NgridParams<R>& p, cudaStream_t s) {
     constexpr auto kern = k_nz_max<R, N, CP, true, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
-    kern<<<nb, NT, smem, s>>>(a, p.twN, zpass_prefetch_distance<R>(kern, NT, smem));
+    kern<<<nb, NT, smem, s>>>(a, p.twN, zpass_prefetch_distance<R, kern>(NT, smem));
   } else {
     constexpr int NT = nz_threads<R, N, CP, false>();
     const size_t smem = (size_t)3 * CP * zpad_len<R>(N) * sizeof(C2<R>);
     constexpr auto kern = k_nz_max<R, N, CP, false, NT>;
     e = prepare_kernel<kern>(smem);
     if (e != cudaSuccess) return e;
-    kern<<<nb, NT, smem, s>>>(a, p.twN, zpass_prefetch_distance<R>(kern, NT, smem));
+    kern<<<nb, NT, smem, s>>>(a, p.twN, zpass_prefetch_distance<R, kern>(NT, smem));
   }
   return cudaGetLastError();
 }

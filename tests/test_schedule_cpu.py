@@ -44,3 +44,17 @@ def test_treeverse_reverses_every_step_within_slots_and_sweeps(checker):
         assert adv_pre == adv - spine_last, (nsteps, nsnap, adv, adv_pre, spine_last)
         if nsnap > 1 and nsteps > 1:
             assert spine_last >= 1
+
+
+def test_binomial_1000_steps_20_slots_advances(checker):
+    """The schedule of the checkpointed-adjoint workload (1000 steps, 20 state
+    slots): 2806 advances in the reversal, 1807 once the forward run has
+    stored the first descent, with every step advanced at most r = 3 times;
+    Griewank's lower bound for 19 free slots, r * l - C(s + r, r - 1) = 2769,
+    is within 2 % of the unstored count."""
+    out = subprocess.run([checker, "1000", "20"], check=True, capture_output=True, text=True).stdout.split()
+    assert out[0] == "ok"
+    adv, r, adv_pre = int(out[2]), int(out[4]), int(out[5])
+    assert (adv, adv_pre, r) == (2806, 1807, 3)
+    bound = r * 1000 - math.comb(19 + r, r - 1)
+    assert bound == 2769 and bound <= adv <= 1.02 * bound

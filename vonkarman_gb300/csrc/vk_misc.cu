@@ -8,7 +8,15 @@ namespace vk {
 // One entry of EtdCoeffs::new (etd.rs:113-135) per integer |k|^2 index m:
 // lambda = -nu k^2, z = lambda dt.  The phi functions are the contour means
 // of etd.rs:15-84; exp(z + cos theta_j) is evaluated as exp(z) exp(cos theta_j)
-// (the second factor precomputed), shared by phi1, phi2 and phi3.
+// (the second factor precomputed), shared by phi1, phi2 and phi3.  The
+// denominators of phi1(z), phi2 and phi3 at a contour point w are |w|^2,
+// |w^2|^2 = |w|^4 and |w^3|^2 = |w|^6, so one reciprocal serves all three
+// (VK_ETD_SHARED_RCP; the FP64 pipe bounds this kernel and a division costs
+// several FP64 instructions): two divisions per point instead of four, each
+// term within a few ulp of the separately divided one.
+#ifndef VK_ETD_SHARED_RCP
+#define VK_ETD_SHARED_RCP 1
+#endif
 __global__ void k_etd_table(double* __restrict__ tab, int nent, double nu, double ks2,
                             const DevScalars* __restrict__ d, int force, ContourConsts cc) {
   if (!force && d->etd_recompute == 0) return;
@@ -35,13 +43,32 @@ __global__ void k_etd_table(double* __restrict__ tab, int nent, double nu, doubl
     const double wre = z + cc.cth[j];
     const double e = ez * cc.exp_cth[j];
     const double ere = e * cc.cos_sth[j], eim = e * cc.sin_sth[j];
+    const double w2re = wre * wre - wim * wim;
+    const double w2im = 2.0 * wre * wim;
+#if VK_ETD_SHARED_RCP
+    const double inv = 1.0 / (wre * wre + wim * wim);
+    const double inv2 = inv * inv;
+    {  // phi1(z)
+      const double nre = ere - 1.0, nim = eim;
+      p1 += (nre * wre + nim * wim) * inv;
+    }
+    {  // phi2(z)
+      const double nre = ere - 1.0 - wre, nim = eim - wim;
+      p2 += (nre * w2re + nim * w2im) * inv2;
+    }
+    {  // phi3(z)
+      const double nre = ere - 1.0 - wre - 0.5 * w2re;
+      const double nim = eim - wim - 0.5 * w2im;
+      const double w3re = wre * w2re - wim * w2im;
+      const double w3im = wre * w2im + wim * w2re;
+      p3 += (nre * w3re + nim * w3im) * (inv2 * inv);
+    }
+#else
     {  // phi1(z)
       const double nre = ere - 1.0, nim = eim;
       const double den = wre * wre + wim * wim;
       p1 += (nre * wre + nim * wim) / den;
     }
-    const double w2re = wre * wre - wim * wim;
-    const double w2im = 2.0 * wre * wim;
     {  // phi2(z)
       const double nre = ere - 1.0 - wre, nim = eim - wim;
       const double den = w2re * w2re + w2im * w2im;
@@ -55,6 +82,7 @@ __global__ void k_etd_table(double* __restrict__ tab, int nent, double nu, doubl
       const double den = w3re * w3re + w3im * w3im;
       p3 += (nre * w3re + nim * w3im) / den;
     }
+#endif
   }
   p1h /= 32.0; p1 /= 32.0; p2 /= 32.0; p3 /= 32.0;
   if (fabs(zh) < 1e-300) p1h = 1.0;

@@ -244,7 +244,10 @@ int vk_profile_read(vk_ctx* ctx, double* ms, int64_t* launches, int32_t n);
 const char* vk_profile_pass_name(int32_t id);
 /* FP64 (fp64 = 1) or FP32 FMA throughput of the device in GFLOP/s. */
 int vk_probe_fma_peak(int32_t device, int32_t fp64, double* gflops);
-/* The context's cudaStream_t. */
+/* The context's cudaStream_t.  Every operation of the context is ordered on
+ * it: a step's ETD table runs on a second stream of the context that forks
+ * from and joins back into this one within the step, so work queued on this
+ * stream after a step (or a wait on it) sees the whole step. */
 int vk_stream(vk_ctx* ctx, void** stream);
 /* Record event slot (0..7) on the context's stream; elapsed device time
  * between two recorded slots (waits for slot b). */

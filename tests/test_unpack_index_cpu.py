@@ -65,3 +65,24 @@ def test_register_unpack_equals_hermitian_split(ns, rad):
     # r * NS < H covers them all
     assert seen == set(range(H))
     assert max(r for r in range(rad) if r * ns < H) == (H - 1) // ns
+
+
+def test_p3f_exchange_index_identities():
+    """k_p3f's exchange layouts (vonkarman_gb300/csrc/vk_p3f.cuh): the inverse
+    exchange puts position p at p + p // 24 (stride LPA = 408 per line), the
+    forward one at p + p // 16 (LPF = 412).  The kernel indexes them with the
+    closed forms below; each must equal the layout and stay inside its line."""
+    LPA, LPF = 408, 412
+    ia = lambda p: p + p // 24
+    iff = lambda p: p + p // 16
+    for j in range(16):            # phase A writes positions 24 j + r
+        for r in range(24):
+            assert ia(24 * j + r) == 25 * j + r < LPA
+    for jp in range(24):           # phase B reads positions jp + 24 r
+        for r in range(16):
+            assert ia(jp + 24 * r) == jp + 25 * r < LPA
+    for j in range(16):            # phase C reads positions j + 16 r
+        for r in range(24):
+            assert iff(j + 16 * r) == j + 17 * r < LPF
+    # the forward exchange fits inside the inverse one (2 column pairs per CTA)
+    assert 6 * LPF <= 12 * LPA

@@ -323,3 +323,46 @@ def test_cox_matthews_variant_is_fourth_order_on_linear_decay():
             s.step()
         errs.append(max(np.abs(a - b).max() for a, b in zip(s.u_hat, ref.u_hat)))
     assert errs[1] < errs[0] / 8.0
+
+
+# vonkarman-core/src/field.rs:147-199  grid_spec_basic / _spectral_shape / _padded / total_points
+def test_grid_spec_basics():
+    from vonkarman_gb300 import GridSpec
+    g = vo.Grid(64)
+    assert abs(g.dx - TWO_PI / 64) < 1e-14 and g.h == 33 and g.m == 96
+    p = GridSpec(64)
+    assert p.spectral_shape == (64, 64, 33) and abs(p.dx - TWO_PI / 64) < 1e-14
+    assert p.padded_3half().n == 96
+    assert GridSpec(32, 1.0).n ** 3 == 32 * 32 * 32
+
+
+# vonkarman-periodic/src/ic/taylor_green.rs:45-52  taylor_green_divergence_free (w = 0)
+def test_taylor_green_w_is_zero():
+    from vonkarman_gb300 import ics
+    assert np.abs(vo.taylor_green(vo.Grid(16))[2]).max() < 1e-14
+    assert np.abs(ics.taylor_green(16)[2]).max() < 1e-14
+
+
+# vonkarman-periodic/src/ic/abc.rs:49-64  abc_divergence_free (finite, w nonzero),
+# :98-126  abc_is_beltrami (curl u = u, so <u . omega> = <|u|^2> = 2 E = 3)
+def test_abc_finite_and_beltrami():
+    g = vo.Grid(32)
+    u = vo.abc_flow(g)
+    phys = [vo.c2r_3d(c, (32, 32, 32)) for c in u]
+    assert all(np.isfinite(p).all() for p in phys)
+    assert np.abs(phys[2]).max() > 0.1
+    s = vo.Periodic3D(g, 0.01, u)
+    assert abs(s.energy() - 1.5) < 1e-6
+    assert abs(s.helicity() - 3.0) < 1e-5
+
+
+# vonkarman-diag/src/scalar.rs:61-86  diagnostics_from_zero_energy, energy_dissipation_identity
+def test_scalar_diagnostics_zero_state_and_rates():
+    from vonkarman_gb300.solver import ScalarDiagnostics
+    rate, _ = ScalarDiagnostics.compute_rates(0.01, 10.0, 5.0)
+    assert abs(rate - (-2.0 * 0.01 * 10.0)) < 1e-14
+    g = vo.Grid(8)
+    zero = [np.zeros((8, 8, 5), np.complex128) for _ in range(3)]
+    d = vo.Periodic3D(g, 0.01, zero).tier1()
+    assert d["energy"] == 0.0 and d["enstrophy"] == 0.0 and d["helicity"] == 0.0
+    assert d["max_vorticity"] == 0.0 and d["energy_dissipation_rate"] == 0.0
